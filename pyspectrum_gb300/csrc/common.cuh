@@ -1,0 +1,67 @@
+// Shared helpers for the pyspectrum_gb300 CUDA library (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+#include <stdio.h>
+#include "../../include/pyspec_gpu.h"
+
+namespace pyspec {
+
+// Records the message returned by pyspec_last_error() for this host thread.
+void set_error(const char* fmt, ...);
+// Adds n to the process-wide count of this library's kernel launches.
+void count_launch(int n = 1);
+// Raises the dynamic shared-memory limit of a kernel once per process.
+int allow_smem(const void* func, size_t bytes);
+
+#define PYSPEC_CHECK_ARG(cond, ...)                          \
+    do {                                                     \
+        if (!(cond)) {                                       \
+            ::pyspec::set_error(__VA_ARGS__);                \
+            return PYSPEC_E_INVALID;                         \
+        }                                                    \
+    } while (0)
+
+#define PYSPEC_CUDA(call)                                                        \
+    do {                                                                         \
+        cudaError_t e_ = (call);                                                 \
+        if (e_ != cudaSuccess) {                                                 \
+            ::pyspec::set_error("%s:%d %s: %s", __FILE__, __LINE__, #call,      \
+                                cudaGetErrorString(e_));                         \
+            return PYSPEC_E_CUDA;                                                \
+        }                                                                        \
+    } while (0)
+
+#define PYSPEC_LAUNCH_CHECK() PYSPEC_CUDA(cudaGetLastError())
+
+#define PYSPEC_TRY(call)              \
+    do {                              \
+        int s_ = (call);              \
+        if (s_ != PYSPEC_OK) return s_; \
+    } while (0)
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Radix plan for the mixed-radix FFTs: N = prod(radix[i]); radices in {2,3,4,5,8}.
+struct RadixPlan {
+    int n;
+    int nstages;
+    int radix[16];
+};
+// Returns false if n has a prime factor > 5.
+bool make_plan(int n, RadixPlan* p);
+
+template <typename T> struct cplx_t;
+template <> struct cplx_t<float> { using type = float2; };
+template <> struct cplx_t<double> { using type = double2; };
+
+template <typename T>
+__host__ __device__ __forceinline__ typename cplx_t<T>::type mk(T x, T y) {
+    typename cplx_t<T>::type r; r.x = x; r.y = y; return r;
+}
+
+// The number of shells is bounded so per-shell tables fit in shared memory.
+constexpr int kMaxShells = 128;
+
+}  // namespace pyspec

@@ -1,0 +1,17 @@
+#pragma once
+#include "common.cuh"
+
+namespace pyspec {
+
+size_t contract_simple_ws(int64_t nvox, int ntri);
+
+template <typename T>
+int contract_simple_impl(const T* fields, int64_t fstride, int nshell, const int32_t* tri, int ntri, const T* wts,
+                         int64_t nvox, double* bsum, double* partials, cudaStream_t st);
+
+// tcgen05 split-BF16 contraction (contract_tc.cu)
+size_t contract_tc_ws(int64_t nvox, int nshell, int ntri);
+int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_t* tri, int ntri, double* bsum,
+                     void* ws, size_t ws_bytes, cudaStream_t st);
+
+}  // namespace pyspec

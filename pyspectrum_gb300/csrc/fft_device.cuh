@@ -1,0 +1,186 @@
+// Mixed-radix Stockham FFT on lines held in shared memory.
+//
+// A tile of `nlines` lines of length n sits in shared memory with element
+// stride `es` and line stride `ls` (in complex elements).  Each stage of radix
+// R reads R elements n/R apart, multiplies by twiddles, applies an R-point
+// DFT and writes them Ns apart into the other buffer (self-sorting, so no bit
+// reversal).  Twiddles come from a per-CTA table tw[m] = exp(sign*2*pi*i*m/n).
+#pragma once
+#include "common.cuh"
+
+namespace pyspec {
+
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+    C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+template <typename C, typename T> __device__ __forceinline__ C cscale(C a, T s) { C r; r.x = a.x * s; r.y = a.y * s; return r; }
+// multiply by sign*i
+template <typename C> __device__ __forceinline__ C cmul_si(C a, int sign) {
+    C r;
+    if (sign > 0) { r.x = -a.y; r.y = a.x; } else { r.x = a.y; r.y = -a.x; }
+    return r;
+}
+
+template <typename T> struct FftConst;
+template <> struct FftConst<float> {
+    static constexpr float s3 = 0.866025403784438647f;   // sin(2pi/3)
+    static constexpr float c51 = 0.309016994374947424f;  // cos(2pi/5)
+    static constexpr float c52 = -0.809016994374947424f; // cos(4pi/5)
+    static constexpr float s51 = 0.951056516295153572f;  // sin(2pi/5)
+    static constexpr float s52 = 0.587785252292473129f;  // sin(4pi/5)
+    static constexpr float r2 = 0.707106781186547524f;   // 1/sqrt(2)
+};
+template <> struct FftConst<double> {
+    static constexpr double s3 = 0.866025403784438647;
+    static constexpr double c51 = 0.309016994374947424;
+    static constexpr double c52 = -0.809016994374947424;
+    static constexpr double s51 = 0.951056516295153572;
+    static constexpr double s52 = 0.587785252292473129;
+    static constexpr double r2 = 0.707106781186547524;
+};
+
+template <typename T, typename C>
+__device__ __forceinline__ void dft2(C* v) {
+    C a = v[0], b = v[1];
+    v[0] = cadd(a, b); v[1] = csub(a, b);
+}
+
+template <typename T, typename C>
+__device__ __forceinline__ void dft3(C* v, int sign) {
+    C a = v[0], b = v[1], c = v[2];
+    C s = cadd(b, c);
+    C d = csub(b, c);
+    C t = csub(a, cscale(s, (T)0.5));
+    C u = cmul_si(cscale(d, FftConst<T>::s3), sign);
+    v[0] = cadd(a, s);
+    v[1] = cadd(t, u);
+    v[2] = csub(t, u);
+}
+
+template <typename T, typename C>
+__device__ __forceinline__ void dft4(C* v, int sign) {
+    C a = v[0], b = v[1], c = v[2], d = v[3];
+    C ac = cadd(a, c), amc = csub(a, c), bd = cadd(b, d);
+    C bmd = cmul_si(csub(b, d), sign);
+    v[0] = cadd(ac, bd);
+    v[2] = csub(ac, bd);
+    v[1] = cadd(amc, bmd);
+    v[3] = csub(amc, bmd);
+}
+
+template <typename T, typename C>
+__device__ __forceinline__ void dft5(C* v, int sign) {
+    C a = v[0];
+    C t1 = cadd(v[1], v[4]), t2 = csub(v[1], v[4]);
+    C t3 = cadd(v[2], v[3]), t4 = csub(v[2], v[3]);
+    C r1 = cadd(a, cadd(cscale(t1, FftConst<T>::c51), cscale(t3, FftConst<T>::c52)));
+    C r2 = cadd(a, cadd(cscale(t1, FftConst<T>::c52), cscale(t3, FftConst<T>::c51)));
+    C i1 = cmul_si(cadd(cscale(t2, FftConst<T>::s51), cscale(t4, FftConst<T>::s52)), sign);
+    C i2 = cmul_si(csub(cscale(t2, FftConst<T>::s52), cscale(t4, FftConst<T>::s51)), sign);
+    v[0] = cadd(a, cadd(t1, t3));
+    v[1] = cadd(r1, i1);
+    v[4] = csub(r1, i1);
+    v[2] = cadd(r2, i2);
+    v[3] = csub(r2, i2);
+}
+
+template <typename T, typename C>
+__device__ __forceinline__ void dft8(C* v, int sign) {
+    C e[4] = {v[0], v[2], v[4], v[6]};
+    C o[4] = {v[1], v[3], v[5], v[7]};
+    dft4<T>(e, sign);
+    dft4<T>(o, sign);
+    const T r2 = FftConst<T>::r2;
+    // o[k] *= exp(sign*2*pi*i*k/8)
+    C w1 = mk<T>(r2, sign * r2), w3 = mk<T>(-r2, sign * r2);
+    o[1] = cmul(o[1], w1);
+    o[2] = cmul_si(o[2], sign);
+    o[3] = cmul(o[3], w3);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        v[k] = cadd(e[k], o[k]);
+        v[k + 4] = csub(e[k], o[k]);
+    }
+}
+
+// Twiddle table tw[m] = exp(sign * 2*pi*i * m / n), m in [0, n).
+template <typename T>
+__device__ __forceinline__ void fill_twiddles(typename cplx_t<T>::type* tw, int n, int sign, int tid, int nthr) {
+    for (int m = tid; m < n; m += nthr) {
+        // reduce the angle to |2m/n| <= 1 before calling sincospi
+        int mm = (2 * m > n) ? m - n : m;
+        T s, c;
+        if constexpr (sizeof(T) == 4) sincospif((2.0f * (float)mm) / (float)n, &s, &c);
+        else sincospi((2.0 * (double)mm) / (double)n, &s, &c);
+        tw[m] = mk<T>(c, sign * s);
+    }
+}
+
+// One Stockham stage over all lines of the tile.  Work items are (butterfly, line);
+// `line_fast` chooses which index varies fastest across threads (pick the one
+// with unit stride in shared memory).
+template <typename T, int R>
+__device__ __forceinline__ void stockham_stage(const typename cplx_t<T>::type* __restrict__ src,
+                                               typename cplx_t<T>::type* __restrict__ dst,
+                                               const typename cplx_t<T>::type* __restrict__ tw,
+                                               int n, int Ns, int nlines, int es, int ls,
+                                               bool line_fast, int sign, int tid, int nthr) {
+    using C = typename cplx_t<T>::type;
+    const int nb = n / R;
+    const int twstep = n / (Ns * R);
+    const int items = nb * nlines;
+    for (int it = tid; it < items; it += nthr) {
+        int j, line;
+        if (line_fast) { line = it % nlines; j = it / nlines; }
+        else { j = it % nb; line = it / nb; }
+        const C* s = src + line * ls;
+        C v[R];
+        const int k = j % Ns;
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = s[(j + r * nb) * es];
+        if (Ns > 1) {
+#pragma unroll
+            for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * k * twstep]);  // r*k < R*Ns, so the index is < n
+        }
+        if constexpr (R == 2) dft2<T>(v);
+        else if constexpr (R == 3) dft3<T>(v, sign);
+        else if constexpr (R == 4) dft4<T>(v, sign);
+        else if constexpr (R == 5) dft5<T>(v, sign);
+        else dft8<T>(v, sign);
+        C* d = dst + line * ls;
+        const int base = (j / Ns) * Ns * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) d[(base + r * Ns) * es] = v[r];
+    }
+}
+
+// Runs the whole plan.  Data starts in buf0; returns the buffer holding the
+// result.  Contains __syncthreads(); all threads of the block must call it.
+template <typename T>
+__device__ typename cplx_t<T>::type* fft_tile(typename cplx_t<T>::type* buf0, typename cplx_t<T>::type* buf1,
+                                             const typename cplx_t<T>::type* tw, const RadixPlan& plan,
+                                             int nlines, int es, int ls, bool line_fast, int sign) {
+    using C = typename cplx_t<T>::type;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    C* src = buf0;
+    C* dst = buf1;
+    int Ns = 1;
+    for (int s = 0; s < plan.nstages; ++s) {
+        const int R = plan.radix[s];
+        switch (R) {
+            case 2: stockham_stage<T, 2>(src, dst, tw, plan.n, Ns, nlines, es, ls, line_fast, sign, tid, nthr); break;
+            case 3: stockham_stage<T, 3>(src, dst, tw, plan.n, Ns, nlines, es, ls, line_fast, sign, tid, nthr); break;
+            case 4: stockham_stage<T, 4>(src, dst, tw, plan.n, Ns, nlines, es, ls, line_fast, sign, tid, nthr); break;
+            case 5: stockham_stage<T, 5>(src, dst, tw, plan.n, Ns, nlines, es, ls, line_fast, sign, tid, nthr); break;
+            default: stockham_stage<T, 8>(src, dst, tw, plan.n, Ns, nlines, es, ls, line_fast, sign, tid, nthr); break;
+        }
+        __syncthreads();
+        C* t = src; src = dst; dst = t;
+        Ns *= R;
+    }
+    return src;
+}
+
+}  // namespace pyspec

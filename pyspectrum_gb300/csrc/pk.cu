@@ -1,0 +1,227 @@
+// Power spectrum: monopole in k_f-wide bins (pyspectrum.py:691-716) and the
+// redshift-space multipoles / P(k, mu) of estimator.f:155-264.
+//
+// Each CTA bins one z-plane into shared-memory histograms (float32 within the
+// plane) and adds them to float64 global bins; a finalize kernel forms the
+// averages.
+#include "common.cuh"
+#include "shells.cuh"
+
+namespace pyspec {
+
+__device__ __forceinline__ int foldi(int i, int n) { return i <= n - i ? i : n - i; }
+
+// Monopole on the reflected grid, summed over the half grid: planes x = 0 and
+// x = N/2 count once, others twice (k and -k); the seven Nyquist corners use
+// the real part only (pyspectrum.py:1149-1156).
+__global__ void pk_mono_kernel(const float2* __restrict__ half, int n, double kf, double* __restrict__ acc) {
+    extern __shared__ double smd[];
+    const int nb = n / 2, nh = n / 2 + 1, hg = n / 2;
+    double* ks = smd;
+    double* ps = smd + nb;
+    unsigned* cnt = reinterpret_cast<unsigned*>(smd + 2 * nb);
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) { ks[i] = 0; ps[i] = 0; cnt[i] = 0; }
+    __syncthreads();
+    const int z = blockIdx.x;
+    const int zf = foldi(z, n);
+    for (int i = threadIdx.x; i < n * nh; i += blockDim.x) {
+        const int y = i / nh, x = i - y * nh;
+        const int yf = foldi(y, n);
+        const int64_t d2 = (int64_t)x * x + (int64_t)yf * yf + (int64_t)zf * zf;
+        const int b = shell_of(d2, 1);
+        if (b < 1 || b > nb) continue;
+        const float2 v = half[((int64_t)z * n + y) * nh + x];
+        const bool corner = (x == 0 || x == hg) && (y == 0 || y == hg) && (z == 0 || z == hg);
+        const float p = corner ? v.x * v.x : v.x * v.x + v.y * v.y;
+        const unsigned wgt = (x == 0 || x == hg) ? 1u : 2u;
+        atomicAdd(&ks[b - 1], (double)wgt * kf * (double)sqrtf((float)d2));
+        atomicAdd(&ps[b - 1], (double)wgt * (double)p);
+        atomicAdd(&cnt[b - 1], wgt);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+        if (cnt[i] == 0) continue;
+        atomicAdd(&acc[i], ks[i]);
+        atomicAdd(&acc[nb + i], ps[i]);
+        atomicAdd(&acc[2 * nb + i], (double)cnt[i]);
+    }
+}
+
+__global__ void pk_mono_finalize(const double* __restrict__ acc, int nb, double kf, double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    const double c = acc[2 * nb + i];
+    const double tp = 2.0 * 3.14159265358979323846;
+    out[i] = c > 0 ? acc[i] / c : 0.0;
+    out[nb + i] = c > 0 ? acc[nb + i] / c / (kf * kf * kf) * (tp * tp * tp) : 0.0;
+    out[2 * nb + i] = c;
+}
+
+// estimator.f:196-244.  Mode selection (imk) is exact integer arithmetic;
+// mu follows the Fortran's single-precision expression order without fused
+// multiply-add, and the mu bin uses float64 exactly as
+// int((abs(mu)+dble(mubin))/dble(mubin)).
+struct RsdConst {
+    float ct, st, cph, sph;   // cos/sin of thetaobs and phiobs (single precision)
+    float kf;                 // tpi/Lbox, single precision
+    float mubin;              // 1./real(Nmu)
+};
+
+__global__ void pk_rsd_kernel(const float2* __restrict__ half, int n, int nbin, int nmu, RsdConst c,
+                              double* __restrict__ acc) {
+    extern __shared__ double sm[];
+    double* b_nk = sm;
+    double* b_k = b_nk + nbin;
+    double* b_p0 = b_k + nbin;
+    double* b_p2 = b_p0 + nbin;
+    double* b_p4 = b_p2 + nbin;
+    double* m_n = b_p4 + nbin;
+    double* m_k = m_n + nbin * nmu;
+    double* m_mu = m_k + nbin * nmu;
+    double* m_p = m_mu + nbin * nmu;
+    const int tot = 5 * nbin + 4 * nbin * nmu;
+    for (int i = threadIdx.x; i < tot; i += blockDim.x) sm[i] = 0;
+    __syncthreads();
+    const int nh = n / 2 + 1;
+    const int iz = blockIdx.x;                         // 0-based z index
+    auto sfreq = [n](int i) { return ((i + n / 2 - 1) % n) - n / 2 + 1; };   // estimator.f:198
+    const int fz = sfreq(iz);
+    const int icz = (n - iz) % n;
+    const double mub = (double)c.mubin;
+    for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+        const int iy = i / n, ix = i - iy * n;
+        const int fy = sfreq(iy), fx = sfreq(ix);
+        const int64_t d2 = (int64_t)fx * fx + (int64_t)fy * fy + (int64_t)fz * fz;
+        const int imk = shell_of(d2, 1);
+        if (imk > nbin || imk == 0) continue;
+        const float rk = __fsqrt_rn((float)d2);
+        const float cot1 = __fdiv_rn((float)fz, rk);
+        const float sit1 = __fsqrt_rn(__fsub_rn(1.0f, __fmul_rn(cot1, cot1)));
+        float cc = 0.0f;
+        if (sit1 > 0.0f) {
+            const float rs = __fmul_rn(rk, sit1);
+            const float cp = __fdiv_rn((float)fx, rs);
+            const float sp = __fdiv_rn((float)fy, rs);
+            cc = __fadd_rn(__fmul_rn(c.sph, sp), __fmul_rn(c.cph, cp));
+        }
+        const float muf = __fadd_rn(__fmul_rn(c.ct, cot1), __fmul_rn(__fmul_rn(c.st, sit1), cc));
+        const double mu = (double)muf;
+        const int imu = (int)((fabs(mu) + mub) / mub);
+        float2 ct;
+        if (ix <= n / 2) ct = half[((int64_t)iz * n + iy) * nh + ix];
+        else ct = half[((int64_t)icz * n + (n - iy) % n) * nh + (n - ix) % n];
+        const float pk = ct.x * ct.x + ct.y * ct.y;
+        const float mu2 = muf * muf;
+        const float le2 = -0.5f + 1.5f * mu2;
+        const float le4 = 0.375f - 3.75f * mu2 + 4.375f * mu2 * mu2;
+        const double kv = (double)__fmul_rn(c.kf, rk);
+        const double pkd = (double)pk;
+        const int b = imk - 1;
+        atomicAdd(&b_nk[b], 1.0);
+        atomicAdd(&b_k[b], kv);
+        atomicAdd(&b_p0[b], pkd);
+        atomicAdd(&b_p2[b], (double)(pk * 5.0f * le2));
+        atomicAdd(&b_p4[b], (double)(pk * 9.0f * le4));
+        if (imu <= nmu && imu > 0) {
+            const int m = b * nmu + imu - 1;
+            atomicAdd(&m_n[m], 1.0);
+            atomicAdd(&m_k[m], kv);
+            atomicAdd(&m_mu[m], fabs(mu));
+            atomicAdd(&m_p[m], pkd);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < tot; i += blockDim.x)
+        if (sm[i] != 0.0) atomicAdd(&acc[i], sm[i]);
+}
+
+__global__ void pk_rsd_finalize(const double* __restrict__ acc, int nbin, int nmu, float kf, double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const double kf3 = (double)((kf * kf) * kf);    // dble(kf**3), single-precision power
+    // acc layout: nk, k, p0, p2, p4 [nbin]; then n, k, mu, p [nbin*nmu]
+    // out layout: k, p0, p2, p4, nk [nbin]; then km, mk, pkm, nkm [nbin*nmu]
+    if (i < nbin) {
+        const double c = acc[i];
+        const bool ok = c > 0;
+        out[i] = ok ? acc[nbin + i] / c : 0.0;
+        out[nbin + i] = ok ? acc[2 * nbin + i] / c / kf3 : 0.0;
+        out[2 * nbin + i] = ok ? acc[3 * nbin + i] / c / kf3 : 0.0;
+        out[3 * nbin + i] = ok ? acc[4 * nbin + i] / c / kf3 : 0.0;
+        out[4 * nbin + i] = c;
+    }
+    if (i < nbin * nmu) {
+        const double* a = acc + 5 * nbin;
+        double* o = out + 5 * nbin;
+        const int M = nbin * nmu;
+        const double c = a[i];
+        const bool ok = c > 0;
+        o[i] = ok ? a[M + i] / c : 0.0;
+        o[M + i] = ok ? a[2 * M + i] / c : 0.0;
+        o[2 * M + i] = ok ? a[3 * M + i] / c / kf3 : 0.0;
+        o[3 * M + i] = c;
+    }
+}
+
+}  // namespace pyspec
+
+using namespace pyspec;
+
+// Both entry points accumulate into the second half of the caller's `out`
+// buffer (zeroed here) and write the finished arrays into the first half, so
+// they need no other memory.
+
+extern "C" int pyspec_pk_monopole(const float* half, int ngrid, double lbox, double* out, void* stream) {
+    PYSPEC_CHECK_ARG(half && out, "NULL pointer");
+    PYSPEC_CHECK_ARG(ngrid >= 4 && ngrid % 2 == 0, "ngrid=%d must be even", ngrid);
+    PYSPEC_CHECK_ARG(lbox > 0, "lbox must be positive");
+    cudaStream_t st = as_stream(stream);
+    const int nb = ngrid / 2;
+    // out holds 3*nb results followed by 3*nb accumulators (6*nb doubles)
+    double* acc = out + 3 * nb;
+    PYSPEC_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * 3 * nb, st));
+    const double kf = 2.0 * 3.14159265358979323846 / lbox;
+    const size_t sm = sizeof(double) * 3 * nb;
+    PYSPEC_TRY(allow_smem((const void*)pk_mono_kernel, sm));
+    pk_mono_kernel<<<ngrid, 256, sm, st>>>(reinterpret_cast<const float2*>(half), ngrid, kf, acc);
+    PYSPEC_LAUNCH_CHECK();
+    pk_mono_finalize<<<(nb + 127) / 128, 128, 0, st>>>(acc, nb, kf, out);
+    PYSPEC_LAUNCH_CHECK();
+    count_launch(2);
+    return PYSPEC_OK;
+}
+
+extern "C" int pyspec_pk_pbox_rsd(const float* half, int ngrid, int irsd, int lbox, int nbin, int nmu,
+                                  double* out, void* stream) {
+    PYSPEC_CHECK_ARG(half && out, "NULL pointer");
+    PYSPEC_CHECK_ARG(ngrid >= 4 && ngrid % 2 == 0, "ngrid=%d must be even", ngrid);
+    PYSPEC_CHECK_ARG(irsd >= 0 && irsd <= 2, "irsd must be 0, 1 or 2");
+    PYSPEC_CHECK_ARG(nbin == ngrid / 2, "nbin must equal ngrid/2");
+    PYSPEC_CHECK_ARG(nmu >= 1 && lbox > 0, "bad nmu or lbox");
+    const size_t tot = 5 * (size_t)nbin + 4 * (size_t)nbin * nmu;
+    const size_t sm = sizeof(double) * tot;
+    PYSPEC_CHECK_ARG(sm <= 200 * 1024, "nbin*nmu too large for one CTA's histogram");
+    cudaStream_t st = as_stream(stream);
+    // out holds the results followed by the accumulators (2*tot doubles)
+    double* acc = out + tot;
+    PYSPEC_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * tot, st));
+    // estimator.f:164-181 in single precision
+    const float pi = 3.141592654f;
+    const float half_pi = 0.5f * pi;
+    const float theta = irsd == 2 ? 0.0f : half_pi;
+    const float phi = irsd == 1 ? half_pi : 0.0f;
+    RsdConst c;
+    c.ct = (float)cos((double)theta);
+    c.st = (float)sin((double)theta);
+    c.cph = (float)cos((double)phi);
+    c.sph = (float)sin((double)phi);
+    c.kf = (2.0f * pi) / (float)lbox;
+    c.mubin = 1.0f / (float)nmu;
+    PYSPEC_TRY(allow_smem((const void*)pk_rsd_kernel, sm));
+    pk_rsd_kernel<<<ngrid, 256, sm, st>>>(reinterpret_cast<const float2*>(half), ngrid, nbin, nmu, c, acc);
+    PYSPEC_LAUNCH_CHECK();
+    const int m = nbin * nmu > nbin ? nbin * nmu : nbin;
+    pk_rsd_finalize<<<(m + 127) / 128, 128, 0, st>>>(acc, nbin, nmu, c.kf, out);
+    PYSPEC_LAUNCH_CHECK();
+    count_launch(2);
+    return PYSPEC_OK;
+}

@@ -1,0 +1,316 @@
+// Shell fields F_j(x) = Re FFT_forward(delta(k) [irk(k) == j]) for every
+// shell j (pyspectrum.py:384-404), as three pruned passes on the half grid:
+//
+//   S1  z-lines : mask by shell, complex FFT along z      (half grid -> work)
+//   S2  y-lines : complex FFT along y                      (work, in place)
+//   S3  x-rows  : complex-to-real FFT along x, sum of F^2  (work -> fields)
+//
+// A mode k = (x, y, z) lies in shell j when d2lo <= x^2 + y'^2 + z'^2 <= d2hi
+// (y' = min(y, N-y)), the exact integer form of int(|k|/step + 0.5) == j.
+// S1 only visits columns (x, y) that can reach the shell; S2 only x blocks
+// with x <= |k|max; S3 treats everything S2 skipped as zero.  Small shells
+// therefore touch a small part of the work grid, which then stays in L2.
+//
+// The C2R step uses the classic half-length trick: for a Hermitian spectrum
+// X[0..N/2] the N real outputs f are, as N/2 complex values, the length-N/2
+// FFT of Z[k] = (X[k] + conj X[N/2-k]) + i e^{-2 pi i k/N} (X[k] - conj X[N/2-k]),
+// with X[0] and X[N/2] replaced by their real parts -- this equals
+// Re(sum over the full grid) for any half grid, which is what the reference's
+// np.real(fftn(...)) computes.
+#include "fft_device.cuh"
+#include "fft3d.cuh"
+#include "shells.cuh"
+
+namespace pyspec {
+
+__host__ __device__ inline int64_t shell_d2lo(int j, int step) {
+    if (j <= 0) return 0;
+    const int64_t a = (int64_t)(2 * j - 1) * step;
+    return (a * a + 3) / 4;            // ceil(a^2/4)
+}
+__host__ __device__ inline int64_t shell_d2hi(int j, int step) {
+    const int64_t a = (int64_t)(2 * j + 1) * step;
+    return (a * a + 3) / 4 - 1;        // ceil(a^2/4) - 1
+}
+
+__device__ __forceinline__ int fold(int i, int n) { return i <= n - i ? i : n - i; }
+
+template <typename T, bool INDICATOR>
+__global__ void __launch_bounds__(256) shell_zpass_kernel(const typename cplx_t<T>::type* __restrict__ half,
+                                                          typename cplx_t<T>::type* __restrict__ work, int n,
+                                                          int64_t d2lo, int64_t d2hi, RadixPlan plan) {
+    using C = typename cplx_t<T>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nh = n / 2 + 1, tx = tile_x<T>();
+    const int ntx = (nh + tx - 1) / tx;
+    const int y = blockIdx.x / ntx;
+    const int x0 = (blockIdx.x % ntx) * tx;
+    const int yf = fold(y, n);
+    if ((int64_t)x0 * x0 + (int64_t)yf * yf > d2hi) return;   // whole tile outside the shell
+    C* tw = reinterpret_cast<C*>(smem_raw);
+    C* buf0 = tw + n;
+    C* buf1 = buf0 + (size_t)tx * n;
+    fill_twiddles<T>(tw, n, -1, threadIdx.x, blockDim.x);
+    const int ncol = min(tx, nh - x0);
+    const int64_t zstride = (int64_t)n * nh;
+    const int64_t base = (int64_t)y * nh + x0;
+    for (int i = threadIdx.x; i < n * tx; i += blockDim.x) {
+        const int z = i / tx, c = i - z * tx;
+        C v = mk<T>(0, 0);
+        if (c < ncol) {
+            const int x = x0 + c, zf = fold(z, n);
+            const int64_t d2 = (int64_t)x * x + (int64_t)yf * yf + (int64_t)zf * zf;
+            if (d2 >= d2lo && d2 <= d2hi) {
+                if constexpr (INDICATOR) v = mk<T>(1, 0);
+                else v = half[base + z * zstride + c];
+            }
+        }
+        buf0[i] = v;
+    }
+    __syncthreads();
+    C* res = fft_tile<T>(buf0, buf1, tw, plan, tx, tx, 1, true, -1);
+    for (int i = threadIdx.x; i < n * tx; i += blockDim.x) {
+        const int z = i / tx, c = i - z * tx;
+        if (c < ncol) work[base + z * zstride + c] = res[i];
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) shell_ypass_kernel(typename cplx_t<T>::type* __restrict__ work, int n,
+                                                          int64_t d2hi, int ntx_active, RadixPlan plan) {
+    using C = typename cplx_t<T>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nh = n / 2 + 1, tx = tile_x<T>();
+    const int z = blockIdx.x / ntx_active;
+    const int x0 = (blockIdx.x % ntx_active) * tx;
+    C* tw = reinterpret_cast<C*>(smem_raw);
+    C* buf0 = tw + n;
+    C* buf1 = buf0 + (size_t)tx * n;
+    fill_twiddles<T>(tw, n, -1, threadIdx.x, blockDim.x);
+    const int ncol = min(tx, nh - x0);
+    const int64_t base = (int64_t)z * n * nh + x0;
+    for (int i = threadIdx.x; i < n * tx; i += blockDim.x) {
+        const int y = i / tx, c = i - y * tx;
+        const int yf = fold(y, n);
+        C v = mk<T>(0, 0);
+        // rows the z pass did not visit hold zeros
+        if (c < ncol && (int64_t)x0 * x0 + (int64_t)yf * yf <= d2hi) v = work[base + (int64_t)y * nh + c];
+        buf0[i] = v;
+    }
+    __syncthreads();
+    C* res = fft_tile<T>(buf0, buf1, tw, plan, tx, tx, 1, true, -1);
+    for (int i = threadIdx.x; i < n * tx; i += blockDim.x) {
+        const int y = i / tx, c = i - y * tx;
+        if (c < ncol) work[base + (int64_t)y * nh + c] = res[i];
+    }
+}
+
+// x rows: RL consecutive rows r = z*n + y per CTA.
+template <typename T>
+__global__ void __launch_bounds__(256) shell_xpass_kernel(const typename cplx_t<T>::type* __restrict__ work, int n,
+                                                          int xlim, int rl, RadixPlan plan_half,
+                                                          T* __restrict__ field, double* __restrict__ part) {
+    using C = typename cplx_t<T>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nh = n / 2 + 1, h = n / 2;
+    C* twN = reinterpret_cast<C*>(smem_raw);   // exp(-2 pi i m / n), m < n
+    C* twH = twN + n;                          // exp(-2 pi i m / (n/2))
+    C* stage = twH + h;                        // rl * nh
+    C* buf0 = stage + (size_t)rl * nh;         // rl * h
+    C* buf1 = buf0 + (size_t)rl * h;
+    __shared__ double red[32];
+    fill_twiddles<T>(twN, n, -1, threadIdx.x, blockDim.x);
+    fill_twiddles<T>(twH, h, -1, threadIdx.x, blockDim.x);
+    const int64_t nrows = (int64_t)n * n;
+    const int64_t r0 = (int64_t)blockIdx.x * rl;
+    const int nr = (int)min((int64_t)rl, nrows - r0);
+    for (int i = threadIdx.x; i < nr * nh; i += blockDim.x) {
+        const int rr = i / nh, x = i - rr * nh;
+        stage[i] = x < xlim ? work[(r0 + rr) * nh + x] : mk<T>(0, 0);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nr * h; i += blockDim.x) {
+        const int rr = i / h, k = i - rr * h;
+        const C* X = stage + rr * nh;
+        C a = X[k], b = X[h - k];
+        if (k == 0) { a.y = 0; b.y = 0; }
+        const C bc = mk<T>(b.x, -b.y);
+        const C e = cadd(a, bc);
+        const C o = cmul(csub(a, bc), twN[k]);
+        buf0[rr * h + k] = mk<T>(e.x - o.y, e.y + o.x);   // e + i*o
+    }
+    __syncthreads();
+    C* res = fft_tile<T>(buf0, buf1, twH, plan_half, nr, 1, h, false, -1);
+    double acc = 0.0;
+    T local = 0;
+    C* out = reinterpret_cast<C*>(field + r0 * n);
+    for (int i = threadIdx.x; i < nr * h; i += blockDim.x) {
+        const C v = res[i];
+        out[i] = v;       // f[2m] = Re z[m], f[2m+1] = Im z[m]; rows are contiguous
+        local += v.x * v.x + v.y * v.y;
+    }
+    acc = (double)local;
+    // block reduction
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) part[blockIdx.x] = v;
+    }
+}
+
+__global__ void reduce_rows_kernel(const double* __restrict__ part, int nper, double* __restrict__ out) {
+    // one block per output; fixed-order tree reduction (deterministic)
+    __shared__ double red[32];
+    const double* p = part + (int64_t)blockIdx.x * nper;
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < nper; i += blockDim.x) acc += p[i];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) out[blockIdx.x] = v;
+    }
+}
+
+static int xpass_rows(int n) { return max(1, min(16, 4096 / n)); }
+
+template <typename T>
+size_t shell_workspace_bytes(int n, int nshell) {
+    using C = typename cplx_t<T>::type;
+    const size_t nh = n / 2 + 1;
+    const int rl = xpass_rows(n);
+    const size_t nblk = ((size_t)n * n + rl - 1) / rl;
+    size_t b = nh * n * n * sizeof(C);
+    b = (b + 255) & ~(size_t)255;
+    b += (size_t)nshell * nblk * sizeof(double);
+    return b;
+}
+
+template <typename T, bool INDICATOR>
+int shell_one_impl(const typename cplx_t<T>::type* half, int n, int step, int j, T* field, double* part,
+                   typename cplx_t<T>::type* work, cudaStream_t st) {
+    using C = typename cplx_t<T>::type;
+    RadixPlan plan, plan_half;
+    PYSPEC_CHECK_ARG(n % 2 == 0 && make_plan(n, &plan) && make_plan(n / 2, &plan_half),
+                     "ngrid=%d must be even and factor into 2, 3 and 5", n);
+    const int nh = n / 2 + 1, tx = tile_x<T>();
+    const int64_t d2lo = shell_d2lo(j, step), d2hi = shell_d2hi(j, step);
+    // largest |kx| that can reach the shell (bounded by the half grid)
+    int kmax = 0;
+    while ((int64_t)(kmax + 1) * (kmax + 1) <= d2hi && kmax + 1 < nh) ++kmax;
+    const int ntx = (nh + tx - 1) / tx;
+    const int ntx_active = min(ntx, kmax / tx + 1);
+    const int xlim = min(nh, ntx_active * tx);
+    const size_t sm_zy = sizeof(C) * ((size_t)n + 2 * (size_t)tx * n);
+    PYSPEC_TRY(allow_smem((const void*)shell_zpass_kernel<T, INDICATOR>, sm_zy));
+    PYSPEC_TRY(allow_smem((const void*)shell_ypass_kernel<T>, sm_zy));
+    shell_zpass_kernel<T, INDICATOR><<<(unsigned)(ntx * n), 256, sm_zy, st>>>(half, work, n, d2lo, d2hi, plan);
+    PYSPEC_LAUNCH_CHECK();
+    shell_ypass_kernel<T><<<(unsigned)(ntx_active * n), 256, sm_zy, st>>>(work, n, d2hi, ntx_active, plan);
+    PYSPEC_LAUNCH_CHECK();
+    const int rl = xpass_rows(n);
+    const int h = n / 2;
+    const size_t sm_x = sizeof(C) * ((size_t)n + h + (size_t)rl * nh + 2 * (size_t)rl * h);
+    PYSPEC_TRY(allow_smem((const void*)shell_xpass_kernel<T>, sm_x));
+    const unsigned nblk = (unsigned)(((int64_t)n * n + rl - 1) / rl);
+    shell_xpass_kernel<T><<<nblk, 256, sm_x, st>>>(work, n, xlim, rl, plan_half, field, part);
+    PYSPEC_LAUNCH_CHECK();
+    count_launch(3);
+    return PYSPEC_OK;
+}
+
+template <typename T, bool INDICATOR>
+int shell_fields_impl(const typename cplx_t<T>::type* half, int n, int step, int jmin, int nmax, T* fields,
+                      double* p0sum, void* ws, size_t ws_bytes, cudaStream_t st) {
+    using C = typename cplx_t<T>::type;
+    const int nshell = nmax - jmin + 1;
+    PYSPEC_CHECK_ARG(nshell >= 1, "nmax < jmin");
+    const size_t need = shell_workspace_bytes<T>(n, nshell);
+    if (ws_bytes < need || ws == nullptr) {
+        set_error("shell workspace %zu bytes < required %zu", ws_bytes, need);
+        return PYSPEC_E_WORKSPACE;
+    }
+    C* work = reinterpret_cast<C*>(ws);
+    const size_t nh = n / 2 + 1;
+    size_t off = (nh * n * n * sizeof(C) + 255) & ~(size_t)255;
+    double* part = reinterpret_cast<double*>(reinterpret_cast<char*>(ws) + off);
+    const int rl = xpass_rows(n);
+    const int nblk = (int)(((int64_t)n * n + rl - 1) / rl);
+    const int64_t V = (int64_t)n * n * n;
+    for (int s = 0; s < nshell; ++s) {
+        PYSPEC_TRY((shell_one_impl<T, INDICATOR>(half, n, step, jmin + s, fields + (int64_t)s * V,
+                                                  part + (int64_t)s * nblk, work, st)));
+    }
+    if (p0sum) {
+        reduce_rows_kernel<<<nshell, 256, 0, st>>>(part, nblk, p0sum);
+        PYSPEC_LAUNCH_CHECK();
+        count_launch();
+    }
+    return PYSPEC_OK;
+}
+
+template size_t shell_workspace_bytes<float>(int, int);
+template size_t shell_workspace_bytes<double>(int, int);
+template int shell_fields_impl<float, false>(const float2*, int, int, int, int, float*, double*, void*, size_t,
+                                             cudaStream_t);
+template int shell_fields_impl<double, true>(const double2*, int, int, int, int, double*, double*, void*,
+                                             size_t, cudaStream_t);
+template int shell_one_impl<double, true>(const double2*, int, int, int, double*, double*, double2*,
+                                          cudaStream_t);
+
+// Nk[j] for j = 0..nmax over the full grid (pyspectrum.py:380)
+__global__ void mode_counts_kernel(int n, int step, int nmax, unsigned long long* __restrict__ nk) {
+    extern __shared__ unsigned long long cnt[];
+    for (int i = threadIdx.x; i <= nmax; i += blockDim.x) cnt[i] = 0;
+    __syncthreads();
+    const int64_t nn = n;
+    const int64_t tot = nn * nn * nn;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (int64_t)gridDim.x * blockDim.x) {
+        const int x = fold((int)(t % nn), n), y = fold((int)((t / nn) % nn), n), z = fold((int)(t / (nn * nn)), n);
+        const int64_t d2 = (int64_t)x * x + (int64_t)y * y + (int64_t)z * z;
+        const int j = shell_of(d2, step);
+        if (j <= nmax) atomicAdd(&cnt[j], 1ull);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i <= nmax; i += blockDim.x)
+        if (cnt[i]) atomicAdd(&nk[i], cnt[i]);
+}
+
+int mode_counts_impl(int n, int step, int nmax, int64_t* nk, cudaStream_t st) {
+    PYSPEC_CUDA(cudaMemsetAsync(nk, 0, sizeof(int64_t) * (nmax + 1), st));
+    mode_counts_kernel<<<608, 256, sizeof(unsigned long long) * (nmax + 1), st>>>(
+        n, step, nmax, reinterpret_cast<unsigned long long*>(nk));
+    PYSPEC_LAUNCH_CHECK();
+    count_launch();
+    return PYSPEC_OK;
+}
+
+}  // namespace pyspec
+
+using namespace pyspec;
+
+extern "C" size_t pyspec_shell_fields_workspace(int ngrid, int nshell) {
+    if (ngrid < 2 || nshell < 1) return 0;
+    return shell_workspace_bytes<float>(ngrid, nshell);
+}
+
+extern "C" int pyspec_shell_fields(const float* half, int ngrid, int step, int jmin, int nmax, float* fields,
+                                   double* p0sum, void* workspace, size_t ws_bytes, void* stream) {
+    PYSPEC_CHECK_ARG(half && fields, "NULL pointer");
+    PYSPEC_CHECK_ARG(ngrid >= 4 && ngrid % 2 == 0 && ngrid <= 2048, "ngrid=%d must be even and <= 2048", ngrid);
+    PYSPEC_CHECK_ARG(step >= 1 && jmin >= 1 && nmax >= jmin, "need step>=1, 1<=jmin<=nmax");
+    PYSPEC_CHECK_ARG(nmax - jmin + 1 <= kMaxShells, "at most %d shells", kMaxShells);
+    return shell_fields_impl<float, false>(reinterpret_cast<const float2*>(half), ngrid, step, jmin, nmax, fields,
+                                           p0sum, workspace, ws_bytes, as_stream(stream));
+}
+
+extern "C" int pyspec_mode_counts(int ngrid, int step, int nmax, int64_t* nk, void* stream) {
+    PYSPEC_CHECK_ARG(nk != nullptr, "NULL pointer");
+    PYSPEC_CHECK_ARG(ngrid >= 2 && step >= 1 && nmax >= 0 && nmax < 4096, "bad arguments");
+    return mode_counts_impl(ngrid, step, nmax, nk, as_stream(stream));
+}

@@ -1,0 +1,35 @@
+"""Host-side logic of the package (no GPU)."""
+import numpy as np
+
+from oracle import pyspec_oracle as O
+from pyspectrum_gb300 import core, util
+
+
+def test_triangle_table_matches_reference_loop():
+    for jmin, nmax in [(1, 5), (1, 40), (2, 7), (1, 60)]:
+        t = core.triangles(jmin, nmax)
+        ref = np.array([(i, j, l) for i, j, l, _ in O.triangles(jmin, nmax)]).T
+        assert np.array_equal(t, ref)
+    assert core.triangles(1, 40).shape[1] == 6350
+    assert core.triangles(1, 60).shape[1] == 20275
+    assert core.triangles(1, 50).shape[1] == 12000
+
+
+def test_rsd_factor_and_applyrsd(golden):
+    g = golden("ref_rsd.npz")
+    for los in "xyz":
+        out = util.applyRSD(g["xyz"], g["vxyz"], 0.5, h=0.7, omega0_m=0.3, LOS=los, Lbox=2600.0)
+        np.testing.assert_allclose(out, g["rsd_" + los], rtol=0, atol=1e-9)
+    assert abs(core.rsd_factor(0.5, 0.3) - 1.5 / (100 * np.sqrt(0.3 * 1.5 ** 3 + 0.7))) < 1e-15
+
+
+def test_ijl_order_groups_by_l_then_j():
+    i = np.array([3, 2, 2, 1]); j = np.array([1, 2, 1, 1]); l = np.array([1, 1, 1, 1])
+    order = util.ijl_order(i, j, l).ravel()
+    assert list(order) == [3, 2, 0, 1]
+
+
+def test_counts_cache_path_naming(tmp_path, monkeypatch):
+    monkeypatch.setenv("PYSPEC_GB300_CACHE", str(tmp_path))
+    p = core.counts_path(360, 40, 3, 3)
+    assert p.startswith(str(tmp_path)) and "Ngrid360.Nmax40.Ncut3.step3" in p
