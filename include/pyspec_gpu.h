@@ -134,13 +134,21 @@ int pyspec_shell_fields(const float *half, int ngrid, int step, int jmin, int nm
 /* ------------------------------------------------------------------------
  * Triangle contraction -- pyspectrum.py:415-437: for every triangle t,
  *   bsum[t] = sum_v fields[i_t][v] * fields[j_t][v] * fields[l_t][v]  (float64 out)
- * tri: int32 device array [3][ntri] of shell SLOTS (0-based rows of fields);
- * a triangle with a slot outside [0, nshell) gets bsum = 0.
- * method: PYSPEC_CONTRACT_FP32 or PYSPEC_CONTRACT_BF16X3.
+ * tri: int32 device array [3][ntri] of shell SLOTS (0-based rows of fields).
+ * tri_host: the same list in host memory, from which both methods plan
+ *   their tiles (plans are cached per list).  Required by
+ *   PYSPEC_CONTRACT_BF16X3; with PYSPEC_CONTRACT_FP32 it may be NULL, which
+ *   selects an unplanned (slower) CUDA-core kernel that reads tri directly.
+ * method: PYSPEC_CONTRACT_FP32 (any nshell <= 128; a triangle with a slot
+ *   outside [0, nshell) gets bsum = 0) or PYSPEC_CONTRACT_BF16X3 (nshell <= 64,
+ *   fields 16-byte aligned, N^3 divisible by 4; returns PYSPEC_E_UNSUPPORTED
+ *   otherwise).  After the stream has run a BF16X3 call, the int32 at
+ *   workspace offset 0 is 0, or the code of a bounded wait that timed out.
  * ---------------------------------------------------------------------- */
 size_t pyspec_bk_contract_workspace(int ngrid, int nshell, int ntri, int method);
-int pyspec_bk_contract(const float *fields, int ngrid, int nshell, const int32_t *tri, int ntri,
-                       int method, double *bsum, void *workspace, size_t ws_bytes, void *stream);
+int pyspec_bk_contract(const float *fields, int ngrid, int nshell, const int32_t *tri,
+                       const int32_t *tri_host, int ntri, int method, double *bsum,
+                       void *workspace, size_t ws_bytes, void *stream);
 
 /* ------------------------------------------------------------------------
  * Triangle counts -- pyspectrum.py:962-1030 (_counts_Bk123) and

@@ -13,6 +13,7 @@ Device layouts
 """
 from __future__ import annotations
 
+import ctypes
 import math
 import os
 import threading
@@ -193,6 +194,7 @@ class BkPlan:
         self.T = tri.shape[1]
         self.tri = torch.from_numpy(tri).to(self.device)
         self.slots = (self.tri - self.jmin).contiguous()
+        self.slots_host = np.ascontiguousarray(tri - self.jmin, dtype=np.int32)
         c, nk = triangle_counts(n, self.nmax, self.ncut, self.step, device=self.device)
         self.counts_np, self.nk_np = c, nk
         self.counts = torch.from_numpy(c).to(self.device)
@@ -209,8 +211,9 @@ class BkPlan:
              ptr(self.p0sum), ptr(self.ws_shell), self.ws_shell.numel(), stream_ptr())
 
     def contract(self):
-        call("pyspec_bk_contract", ptr(self.fields), self.n, self.S, ptr(self.slots), self.T,
-             METHODS[self.method], ptr(self.bsum), ptr(self.ws_con), self.ws_con.numel(), stream_ptr())
+        call("pyspec_bk_contract", ptr(self.fields), self.n, self.S, ptr(self.slots),
+             self.slots_host.ctypes.data_as(ctypes.c_void_p), self.T, METHODS[self.method], ptr(self.bsum),
+             ptr(self.ws_con), self.ws_con.numel(), stream_ptr())
 
     def normalize(self, apply_units=False, nbar=1.0, kf=1.0):
         call("pyspec_bk_normalize", ptr(self.bsum), ptr(self.counts), ptr(self.p0sum), ptr(self.nk),

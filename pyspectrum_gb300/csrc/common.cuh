@@ -43,11 +43,34 @@ int allow_smem(const void* func, size_t bytes);
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Exact unsigned division by a runtime constant d (Granlund-Montgomery):
+// q = (umulhi(m, x) + x) >> l for all x < 2^31.
+struct FastDiv {
+    uint32_t m;
+    int l;
+    uint32_t d;
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+    FastDiv f;
+    f.d = d;
+    int l = 0;
+    while ((1ull << l) < d) ++l;
+    f.l = l;
+    f.m = (uint32_t)((((1ull << l) - d) << 32) / d + 1);
+    return f;
+}
+__device__ __forceinline__ uint32_t fdiv(uint32_t x, const FastDiv& f) {
+    return (__umulhi(f.m, x) + x) >> f.l;
+}
+
 // Radix plan for the mixed-radix FFTs: N = prod(radix[i]); radices in {2,3,4,5,8}.
+// ns[s] = product of the radices before stage s; nb[s] = n / radix[s].
 struct RadixPlan {
     int n;
     int nstages;
     int radix[16];
+    FastDiv ns[16];
+    FastDiv nb[16];
 };
 // Returns false if n has a prime factor > 5.
 bool make_plan(int n, RadixPlan* p);

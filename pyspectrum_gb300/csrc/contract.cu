@@ -9,6 +9,10 @@
 // folded into a Kahan-compensated float32 running sum; each CTA writes one
 // float64 partial per triangle and a second kernel adds the CTA partials in a
 // fixed order (float64, deterministic).
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <vector>
 #include "common.cuh"
 #include "contract.cuh"
 #include "shells.cuh"
@@ -112,9 +116,14 @@ int contract_simple_impl(const T* fields, int64_t fstride, int nshell, const int
     contract_simple_kernel<T><<<dim3(gx, gy), kCthreads, sm, st>>>(fields, fstride, nshell, tri, ntri, wts, nvox,
                                                                    partials);
     PYSPEC_LAUNCH_CHECK();
-    reduce_partials_kernel<<<(ntri + 255) / 256, 256, 0, st>>>(partials, (int)gx, ntri, bsum);
+    count_launch();
+    return reduce_partials_launch(partials, (int)gx, ntri, bsum, st);
+}
+
+int reduce_partials_launch(const double* partials, int nblk, int ntri, double* bsum, cudaStream_t st) {
+    reduce_partials_kernel<<<(ntri + 255) / 256, 256, 0, st>>>(partials, nblk, ntri, bsum);
     PYSPEC_LAUNCH_CHECK();
-    count_launch(2);
+    count_launch();
     return PYSPEC_OK;
 }
 
@@ -122,6 +131,258 @@ template int contract_simple_impl<float>(const float*, int64_t, int, const int32
                                          double*, double*, cudaStream_t);
 template int contract_simple_impl<double>(const double*, int64_t, int, const int32_t*, int, const double*, int64_t,
                                           double*, double*, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// FP32 CUDA-core contraction, register-tiled.  Triangles are grouped as
+// (pair (i, j), shell l) like the tensor-core form: pairs sorted by (j, i),
+// four consecutive pairs x eight consecutive l form one thread's micro-tile
+// (32 accumulators).  Per voxel pair a thread loads 16 float2 values, forms 4
+// pair products and issues 32 packed FP32x2 FMAs.  Voxel chunks are staged in
+// shared memory with cp.async (double-buffered); each chunk's FP32 sums are
+// folded into Kahan-compensated FP32 totals; CTAs write float64 partials.
+// ---------------------------------------------------------------------------
+namespace simt {
+constexpr int MT = 4, NT = 8, VC = 128, FS = VC + 2;   // padded row of the staging buffer
+constexpr int MAXT = 384;                               // micro-tiles per CTA (threads; 168 registers each)
+
+struct Params {
+    const float* fields;
+    int64_t V;
+    int nshell;
+    int ntile;                 // micro-tiles
+    int tiles_per_cta;         // threads per CTA (multiple of 32)
+    const int16_t* tile_rows;  // [ntile][8]: i0..i3, j0..j3 (slot, -1 = empty row)
+    const int16_t* tile_l0;    // [ntile]
+    const int32_t* tile_tri;   // [ntile][32] triangle index or -1
+    int ntri;
+    int64_t nchunks, chunks_per_cta;
+    double* partials;          // [gridDim.x][ntri]
+};
+
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    float2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(*reinterpret_cast<unsigned long long*>(&r))
+        : "l"(*reinterpret_cast<unsigned long long*>(&a)), "l"(*reinterpret_cast<unsigned long long*>(&b)),
+          "l"(*reinterpret_cast<unsigned long long*>(&c)));
+    return r;
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+    float2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(*reinterpret_cast<unsigned long long*>(&r))
+        : "l"(*reinterpret_cast<unsigned long long*>(&a)), "l"(*reinterpret_cast<unsigned long long*>(&b)));
+    return r;
+}
+
+__global__ void __launch_bounds__(MAXT, 1) contract_fp32_kernel(const __grid_constant__ Params P) {
+    extern __shared__ __align__(16) float sbuf[];       // 2 x (nshell + NT) x FS
+    const int tid = threadIdx.x;
+    const int rowsz = (P.nshell + NT) * FS;
+    const int tile = blockIdx.y * P.tiles_per_cta + tid;
+    const bool valid = tid < P.tiles_per_cta && tile < P.ntile;
+    const int zero_row = P.nshell * FS;                  // never written by the copies
+    // rows nshell .. nshell+NT-1 of both buffers are zero and never copied into
+    for (int i = tid; i < NT * FS; i += blockDim.x) { sbuf[zero_row + i] = 0.f; sbuf[rowsz + zero_row + i] = 0.f; }
+    int fi[MT], fj[MT];
+#pragma unroll
+    for (int k = 0; k < MT; ++k) {
+        const int i = valid ? P.tile_rows[(size_t)tile * 8 + k] : -1;
+        const int j = valid ? P.tile_rows[(size_t)tile * 8 + 4 + k] : -1;
+        fi[k] = i >= 0 ? i * FS : zero_row;
+        fj[k] = j >= 0 ? j * FS : zero_row;
+    }
+    // l0 + m <= nshell + NT - 1 always stays inside the buffer
+    const int fl0 = (valid ? P.tile_l0[tile] : P.nshell) * FS;
+    float hi[MT * NT], lo[MT * NT];
+#pragma unroll
+    for (int e = 0; e < MT * NT; ++e) { hi[e] = 0.f; lo[e] = 0.f; }
+
+    const int64_t c0 = (int64_t)blockIdx.x * P.chunks_per_cta;
+    const int64_t c1 = min(P.nchunks, c0 + P.chunks_per_cta);
+    const int nch = (int)max((int64_t)0, c1 - c0);
+    const int ncp = P.nshell * (VC / 4);
+    auto issue = [&](int c, int buf) {
+        const int64_t vbase = (c0 + c) * VC;
+        for (int u = tid; u < ncp; u += blockDim.x) {
+            const int s = u / (VC / 4), q = u - s * (VC / 4);
+            const int64_t v = vbase + 4 * q;
+            int bytes = 0;
+            if (v < P.V) bytes = (int)min((int64_t)16, (P.V - v) * 4);
+            const float* src = P.fields + (size_t)s * P.V + (bytes > 0 ? v : 0);
+            const uint32_t dst = (uint32_t)__cvta_generic_to_shared(sbuf + buf * rowsz + s * FS + 4 * q);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" :: "r"(dst), "l"(src),
+                         "r"(bytes > 8 ? 8 : bytes) : "memory");
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" :: "r"(dst + 8), "l"(src + 2),
+                         "r"(bytes > 8 ? bytes - 8 : 0) : "memory");
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    if (nch > 0) issue(0, 0);
+    for (int c = 0; c < nch; ++c) {
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncthreads();
+        if (c + 1 < nch) issue(c + 1, (c + 1) & 1);
+        const float* F = sbuf + (c & 1) * rowsz;
+        float2 cur[MT * NT];
+#pragma unroll
+        for (int e = 0; e < MT * NT; ++e) cur[e] = make_float2(0.f, 0.f);
+        if (valid) {
+#pragma unroll 2
+            for (int v = 0; v < VC; v += 2) {
+                float2 pp[MT], ll[NT];
+#pragma unroll
+                for (int k = 0; k < MT; ++k)
+                    pp[k] = mul2(*reinterpret_cast<const float2*>(F + fi[k] + v),
+                                 *reinterpret_cast<const float2*>(F + fj[k] + v));
+#pragma unroll
+                for (int m = 0; m < NT; ++m) ll[m] = *reinterpret_cast<const float2*>(F + fl0 + m * FS + v);
+#pragma unroll
+                for (int k = 0; k < MT; ++k)
+#pragma unroll
+                    for (int m = 0; m < NT; ++m) cur[k * NT + m] = fma2(pp[k], ll[m], cur[k * NT + m]);
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < MT * NT; ++e) {   // Kahan fold of the chunk sum
+            const float y = (cur[e].x + cur[e].y) - lo[e];
+            const float t = hi[e] + y;
+            lo[e] = (t - hi[e]) - y;
+            hi[e] = t;
+        }
+        __syncthreads();   // everyone is done with buffer c&1 before it is refilled
+    }
+    if (valid) {
+#pragma unroll
+        for (int e = 0; e < MT * NT; ++e) {
+            const int t = P.tile_tri[(size_t)tile * 32 + e];
+            if (t >= 0) P.partials[(size_t)blockIdx.x * P.ntri + t] = (double)hi[e] - (double)lo[e];
+        }
+    }
+}
+
+struct HostPlan {
+    std::vector<int16_t> rows, l0;
+    std::vector<int32_t> tri;
+    int ntile = 0;
+    bool ok = false;
+};
+
+static std::mutex g_mu;
+static std::map<std::vector<int32_t>, HostPlan*> g_plans;
+
+static HostPlan* plan(int nshell, const int32_t* tri_host, int ntri) {
+    std::vector<int32_t> key(tri_host, tri_host + 3 * (size_t)ntri);
+    key.push_back(nshell);
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_plans.find(key);
+    if (it != g_plans.end()) return it->second;
+    HostPlan* hp = new HostPlan();
+    std::map<std::pair<int, int>, std::vector<std::pair<int, int>>> pairs;
+    bool ok = true;
+    for (int t = 0; t < ntri; ++t) {
+        int v[3] = {tri_host[t], tri_host[ntri + t], tri_host[2 * ntri + t]};
+        if (v[0] < 0 || v[1] < 0 || v[2] < 0 || v[0] >= nshell || v[1] >= nshell || v[2] >= nshell) continue;
+        std::sort(v, v + 3);
+        pairs[{v[2], v[1]}].push_back({v[0], t});
+    }
+    std::vector<std::pair<int, int>> order;
+    for (auto& kv : pairs) order.push_back(kv.first);
+    std::sort(order.begin(), order.end(), [](const std::pair<int, int>& a, const std::pair<int, int>& b) {
+        return a.second != b.second ? a.second < b.second : a.first < b.first;
+    });
+    for (size_t g = 0; g < order.size(); g += MT) {
+        int lo = 1 << 30, hi = -1;
+        for (size_t r = g; r < std::min(order.size(), g + MT); ++r)
+            for (auto& lt : pairs[order[r]]) { lo = std::min(lo, lt.first); hi = std::max(hi, lt.first); }
+        for (int l0 = lo; l0 <= hi; l0 += NT) {
+            int16_t rr[8];
+            int32_t tt[32];
+            for (int e = 0; e < 32; ++e) tt[e] = -1;
+            for (int k = 0; k < MT; ++k) {
+                const size_t r = g + k;
+                rr[k] = r < order.size() ? (int16_t)order[r].first : (int16_t)-1;
+                rr[4 + k] = r < order.size() ? (int16_t)order[r].second : (int16_t)-1;
+                if (r >= order.size()) continue;
+                for (auto& lt : pairs[order[r]])
+                    if (lt.first >= l0 && lt.first < l0 + NT) tt[k * NT + lt.first - l0] = lt.second;
+            }
+            hp->rows.insert(hp->rows.end(), rr, rr + 8);
+            hp->l0.push_back((int16_t)l0);
+            hp->tri.insert(hp->tri.end(), tt, tt + 32);
+            ++hp->ntile;
+        }
+    }
+    hp->ok = ok;
+    g_plans[key] = hp;
+    return hp;
+}
+
+static size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
+
+static void grid_dims(int64_t nvox, int ntile, int* gx, int* gy, int* per) {
+    *gy = std::max(1, (ntile + MAXT - 1) / MAXT);
+    *per = ((ntile + *gy - 1) / *gy + 31) / 32 * 32;
+    int sms = 152, dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t nch = (nvox + VC - 1) / VC;
+    *gx = (int)std::max<int64_t>(1, std::min<int64_t>(nch, std::max(1, sms / *gy)));
+}
+
+}  // namespace simt
+
+size_t contract_fp32_ws(int64_t nvox, int nshell, int ntri) {
+    // worst-case tile count: one tile per (pair row, l group) with all pairs distinct
+    const size_t maxtile = (size_t)std::max(1, ntri);
+    const size_t tables = simt::al(maxtile * 16) + simt::al(maxtile * 2) + simt::al(maxtile * 128);
+    int sms = 152, dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    (void)nshell;
+    (void)nvox;
+    return tables + simt::al((size_t)sms * std::max(ntri, 1) * sizeof(double)) + 256;
+}
+
+int contract_fp32_impl(const float* fields, int64_t nvox, int nshell, const int32_t* tri_host, int ntri,
+                       double* bsum, void* ws, size_t ws_bytes, cudaStream_t st) {
+    using namespace simt;
+    PYSPEC_CHECK_ARG(tri_host != nullptr, "the FP32 contraction needs the host copy of the triangle list");
+    PYSPEC_CHECK_ARG(nvox % 4 == 0 && ((uintptr_t)fields & 15) == 0, "fields must be 16-byte aligned, N^3 % 4 == 0");
+    HostPlan* hp = plan(nshell, tri_host, ntri);
+    int gx, gy, per;
+    grid_dims(nvox, hp->ntile, &gx, &gy, &per);
+    char* w = reinterpret_cast<char*>(ws);
+    size_t off = 0;
+    int16_t* d_rows = reinterpret_cast<int16_t*>(w + off); off += al(hp->rows.size() * 2);
+    int16_t* d_l0 = reinterpret_cast<int16_t*>(w + off); off += al(hp->l0.size() * 2);
+    int32_t* d_tri = reinterpret_cast<int32_t*>(w + off); off += al(hp->tri.size() * 4);
+    double* partials = reinterpret_cast<double*>(w + off);
+    off += al((size_t)gx * ntri * sizeof(double));
+    if (off > ws_bytes) {
+        set_error("contract workspace %zu bytes < required %zu", ws_bytes, off);
+        return PYSPEC_E_WORKSPACE;
+    }
+    PYSPEC_CUDA(cudaMemcpyAsync(d_rows, hp->rows.data(), hp->rows.size() * 2, cudaMemcpyHostToDevice, st));
+    PYSPEC_CUDA(cudaMemcpyAsync(d_l0, hp->l0.data(), hp->l0.size() * 2, cudaMemcpyHostToDevice, st));
+    PYSPEC_CUDA(cudaMemcpyAsync(d_tri, hp->tri.data(), hp->tri.size() * 4, cudaMemcpyHostToDevice, st));
+    PYSPEC_CUDA(cudaMemsetAsync(partials, 0, (size_t)gx * ntri * sizeof(double), st));
+    Params P;
+    P.fields = fields;
+    P.V = nvox;
+    P.nshell = nshell;
+    P.ntile = hp->ntile;
+    P.tiles_per_cta = per;
+    P.tile_rows = d_rows;
+    P.tile_l0 = d_l0;
+    P.tile_tri = d_tri;
+    P.ntri = ntri;
+    P.nchunks = (nvox + VC - 1) / VC;
+    P.chunks_per_cta = (P.nchunks + gx - 1) / gx;
+    P.partials = partials;
+    const size_t sm = sizeof(float) * 2 * (size_t)(nshell + NT) * FS;
+    PYSPEC_TRY(allow_smem((const void*)contract_fp32_kernel, sm));
+    contract_fp32_kernel<<<dim3(gx, gy), per, sm, st>>>(P);
+    PYSPEC_LAUNCH_CHECK();
+    count_launch();
+    return reduce_partials_launch(partials, gx, ntri, bsum, st);
+}
 
 // ---------------------------------------------------------------------------
 // Triangle counts.  The shell indicator fields I_j are invariant under
@@ -320,11 +581,12 @@ extern "C" size_t pyspec_bk_contract_workspace(int ngrid, int nshell, int ntri, 
     if (ngrid < 2 || nshell < 1 || ntri < 0) return 0;
     const int64_t V = (int64_t)ngrid * ngrid * ngrid;
     if (method == PYSPEC_CONTRACT_BF16X3) return contract_tc_ws(V, nshell, ntri);
-    return contract_simple_ws(V, ntri);
+    return std::max(contract_fp32_ws(V, nshell, ntri), contract_simple_ws(V, ntri));
 }
 
-extern "C" int pyspec_bk_contract(const float* fields, int ngrid, int nshell, const int32_t* tri, int ntri,
-                                  int method, double* bsum, void* workspace, size_t ws_bytes, void* stream) {
+extern "C" int pyspec_bk_contract(const float* fields, int ngrid, int nshell, const int32_t* tri,
+                                  const int32_t* tri_host, int ntri, int method, double* bsum, void* workspace,
+                                  size_t ws_bytes, void* stream) {
     PYSPEC_CHECK_ARG(fields && tri && bsum, "NULL pointer");
     PYSPEC_CHECK_ARG(ngrid >= 2 && nshell >= 1 && nshell <= kMaxShells && ntri >= 0, "bad arguments");
     if (ntri == 0) return PYSPEC_OK;
@@ -335,11 +597,14 @@ extern "C" int pyspec_bk_contract(const float* fields, int ngrid, int nshell, co
         return PYSPEC_E_WORKSPACE;
     }
     cudaStream_t st = as_stream(stream);
-    if (method == PYSPEC_CONTRACT_FP32)
-        return contract_simple_impl<float>(fields, V, nshell, tri, ntri, nullptr, V, bsum,
-                                           reinterpret_cast<double*>(workspace), st);
+    if (method == PYSPEC_CONTRACT_FP32) {
+        if (tri_host == nullptr)   // device-only triangle list: the unplanned kernel
+            return contract_simple_impl<float>(fields, V, nshell, tri, ntri, nullptr, V, bsum,
+                                               reinterpret_cast<double*>(workspace), st);
+        return contract_fp32_impl(fields, V, nshell, tri_host, ntri, bsum, workspace, ws_bytes, st);
+    }
     if (method == PYSPEC_CONTRACT_BF16X3)
-        return contract_tc_impl(fields, V, nshell, tri, ntri, bsum, workspace, ws_bytes, st);
+        return contract_tc_impl(fields, V, nshell, tri, tri_host, ntri, bsum, workspace, ws_bytes, st);
     set_error("unknown contraction method %d", method);
     return PYSPEC_E_INVALID;
 }

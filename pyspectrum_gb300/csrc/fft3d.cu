@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(256) fft_contig_kernel(typename cplx_t<T>::typ
     const int cnt = nl * n;
     for (int i = threadIdx.x; i < cnt; i += blockDim.x) buf0[i] = g[i];
     __syncthreads();
-    C* res = fft_tile<T>(buf0, buf1, tw, plan, nl, 1, n, false, sign);
+    C* res = fft_tile<T, 0>(buf0, buf1, tw, plan, nl, sign);
     for (int i = threadIdx.x; i < cnt; i += blockDim.x) g[i] = res[i];
 }
 
@@ -37,8 +37,9 @@ __global__ void __launch_bounds__(256) fft_contig_kernel(typename cplx_t<T>::typ
 // Tile b covers outer index b / ntx and x block b % ntx.
 template <typename T>
 __global__ void __launch_bounds__(256) fft_strided_kernel(typename cplx_t<T>::type* data, int nx, int64_t row_stride,
-                                                          int64_t outer_stride, int tx, RadixPlan plan, int sign) {
+                                                          int64_t outer_stride, RadixPlan plan, int sign) {
     using C = typename cplx_t<T>::type;
+    constexpr int tx = tile_x<T>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = plan.n;
     C* tw = reinterpret_cast<C*>(smem_raw);
@@ -56,7 +57,7 @@ __global__ void __launch_bounds__(256) fft_strided_kernel(typename cplx_t<T>::ty
         if (c < ncol) buf0[i] = g[r * row_stride + c];
     }
     __syncthreads();
-    C* res = fft_tile<T>(buf0, buf1, tw, plan, tx, tx, 1, true, sign);
+    C* res = fft_tile<T, tx>(buf0, buf1, tw, plan, tx, sign);
     for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
         const int r = i / tx, c = i - r * tx;
         if (c < ncol) g[r * row_stride + c] = res[i];
@@ -85,9 +86,9 @@ int fft3d_c2c_impl(typename cplx_t<T>::type* data, int n, int sign, cudaStream_t
     const int ntx = (n + tx - 1) / tx;
     size_t sm = sizeof(C) * ((size_t)n + 2 * (size_t)tx * n);
     PYSPEC_TRY(allow_smem((const void*)fft_strided_kernel<T>, sm));
-    fft_strided_kernel<T><<<(unsigned)(ntx * n), 256, sm, st>>>(data, n, n, (int64_t)n * n, tx, plan, sign);
+    fft_strided_kernel<T><<<(unsigned)(ntx * n), 256, sm, st>>>(data, n, n, (int64_t)n * n, plan, sign);
     PYSPEC_LAUNCH_CHECK();
-    fft_strided_kernel<T><<<(unsigned)(ntx * n), 256, sm, st>>>(data, n, (int64_t)n * n, n, tx, plan, sign);
+    fft_strided_kernel<T><<<(unsigned)(ntx * n), 256, sm, st>>>(data, n, (int64_t)n * n, n, plan, sign);
     PYSPEC_LAUNCH_CHECK();
     count_launch(2);
     return PYSPEC_OK;

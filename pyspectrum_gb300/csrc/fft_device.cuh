@@ -118,26 +118,31 @@ __device__ __forceinline__ void fill_twiddles(typename cplx_t<T>::type* tw, int 
     }
 }
 
-// One Stockham stage over all lines of the tile.  Work items are (butterfly, line);
-// `line_fast` chooses which index varies fastest across threads (pick the one
-// with unit stride in shared memory).
-template <typename T, int R>
+// One Stockham stage over all lines of the tile.  Work items are (butterfly,
+// line).  With LINES > 0 (compile time, a power of two) the line index varies
+// fastest across threads -- the layout of the strided passes, whose lines have
+// unit stride in shared memory; with LINES == 0 the butterfly index varies
+// fastest (contiguous lines).  All index arithmetic is shifts or
+// multiply-high divisions.
+template <typename T, int R, int LINES>
 __device__ __forceinline__ void stockham_stage(const typename cplx_t<T>::type* __restrict__ src,
                                                typename cplx_t<T>::type* __restrict__ dst,
                                                const typename cplx_t<T>::type* __restrict__ tw,
-                                               int n, int Ns, int nlines, int es, int ls,
-                                               bool line_fast, int sign, int tid, int nthr) {
+                                               int n, const FastDiv& nsd, const FastDiv& nbd, int nlines, int es,
+                                               int ls, int sign, int tid, int nthr) {
     using C = typename cplx_t<T>::type;
-    const int nb = n / R;
-    const int twstep = n / (Ns * R);
-    const int items = nb * nlines;
+    const int nb = (int)nbd.d;
+    const int Ns = (int)nsd.d;
+    const int twstep = nb / Ns;      // n / (Ns * R)
+    const int items = nb * (LINES > 0 ? LINES : nlines);
     for (int it = tid; it < items; it += nthr) {
         int j, line;
-        if (line_fast) { line = it % nlines; j = it / nlines; }
-        else { j = it % nb; line = it / nb; }
+        if constexpr (LINES > 0) { line = it & (LINES - 1); j = it / LINES; }
+        else { line = (int)fdiv((uint32_t)it, nbd); j = it - line * nb; }
         const C* s = src + line * ls;
         C v[R];
-        const int k = j % Ns;
+        const int jb = (int)fdiv((uint32_t)j, nsd);
+        const int k = j - jb * Ns;
 #pragma unroll
         for (int r = 0; r < R; ++r) v[r] = s[(j + r * nb) * es];
         if (Ns > 1) {
@@ -150,7 +155,7 @@ __device__ __forceinline__ void stockham_stage(const typename cplx_t<T>::type* _
         else if constexpr (R == 5) dft5<T>(v, sign);
         else dft8<T>(v, sign);
         C* d = dst + line * ls;
-        const int base = (j / Ns) * Ns * R + k;
+        const int base = jb * Ns * R + k;
 #pragma unroll
         for (int r = 0; r < R; ++r) d[(base + r * Ns) * es] = v[r];
     }
@@ -158,27 +163,29 @@ __device__ __forceinline__ void stockham_stage(const typename cplx_t<T>::type* _
 
 // Runs the whole plan.  Data starts in buf0; returns the buffer holding the
 // result.  Contains __syncthreads(); all threads of the block must call it.
-template <typename T>
+// LINES > 0: LINES lines with element stride LINES (line stride 1);
+// LINES == 0: nlines contiguous lines of length plan.n.
+template <typename T, int LINES>
 __device__ typename cplx_t<T>::type* fft_tile(typename cplx_t<T>::type* buf0, typename cplx_t<T>::type* buf1,
                                              const typename cplx_t<T>::type* tw, const RadixPlan& plan,
-                                             int nlines, int es, int ls, bool line_fast, int sign) {
+                                             int nlines, int sign) {
     using C = typename cplx_t<T>::type;
     const int tid = threadIdx.x, nthr = blockDim.x;
+    const int es = LINES > 0 ? LINES : 1;
+    const int ls = LINES > 0 ? 1 : plan.n;
     C* src = buf0;
     C* dst = buf1;
-    int Ns = 1;
     for (int s = 0; s < plan.nstages; ++s) {
         const int R = plan.radix[s];
         switch (R) {
-            case 2: stockham_stage<T, 2>(src, dst, tw, plan.n, Ns, nlines, es, ls, line_fast, sign, tid, nthr); break;
-            case 3: stockham_stage<T, 3>(src, dst, tw, plan.n, Ns, nlines, es, ls, line_fast, sign, tid, nthr); break;
-            case 4: stockham_stage<T, 4>(src, dst, tw, plan.n, Ns, nlines, es, ls, line_fast, sign, tid, nthr); break;
-            case 5: stockham_stage<T, 5>(src, dst, tw, plan.n, Ns, nlines, es, ls, line_fast, sign, tid, nthr); break;
-            default: stockham_stage<T, 8>(src, dst, tw, plan.n, Ns, nlines, es, ls, line_fast, sign, tid, nthr); break;
+            case 2: stockham_stage<T, 2, LINES>(src, dst, tw, plan.n, plan.ns[s], plan.nb[s], nlines, es, ls, sign, tid, nthr); break;
+            case 3: stockham_stage<T, 3, LINES>(src, dst, tw, plan.n, plan.ns[s], plan.nb[s], nlines, es, ls, sign, tid, nthr); break;
+            case 4: stockham_stage<T, 4, LINES>(src, dst, tw, plan.n, plan.ns[s], plan.nb[s], nlines, es, ls, sign, tid, nthr); break;
+            case 5: stockham_stage<T, 5, LINES>(src, dst, tw, plan.n, plan.ns[s], plan.nb[s], nlines, es, ls, sign, tid, nthr); break;
+            default: stockham_stage<T, 8, LINES>(src, dst, tw, plan.n, plan.ns[s], plan.nb[s], nlines, es, ls, sign, tid, nthr); break;
         }
         __syncthreads();
         C* t = src; src = dst; dst = t;
-        Ns *= R;
     }
     return src;
 }

@@ -30,7 +30,14 @@ bool make_plan(int n, RadixPlan* p) {
             m /= order[k];
         }
     }
-    return m == 1 && n >= 2;
+    if (m != 1 || n < 2) return false;
+    int ns = 1;
+    for (int s = 0; s < p->nstages; ++s) {
+        p->ns[s] = make_fastdiv((uint32_t)ns);
+        p->nb[s] = make_fastdiv((uint32_t)(n / p->radix[s]));
+        ns *= p->radix[s];
+    }
+    return true;
 }
 
 }  // namespace pyspec

@@ -41,7 +41,8 @@ __global__ void __launch_bounds__(256) shell_zpass_kernel(const typename cplx_t<
                                                           int64_t d2lo, int64_t d2hi, RadixPlan plan) {
     using C = typename cplx_t<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int nh = n / 2 + 1, tx = tile_x<T>();
+    const int nh = n / 2 + 1;
+    constexpr int tx = tile_x<T>();
     const int ntx = (nh + tx - 1) / tx;
     const int y = blockIdx.x / ntx;
     const int x0 = (blockIdx.x % ntx) * tx;
@@ -68,7 +69,7 @@ __global__ void __launch_bounds__(256) shell_zpass_kernel(const typename cplx_t<
         buf0[i] = v;
     }
     __syncthreads();
-    C* res = fft_tile<T>(buf0, buf1, tw, plan, tx, tx, 1, true, -1);
+    C* res = fft_tile<T, tx>(buf0, buf1, tw, plan, tx, -1);
     for (int i = threadIdx.x; i < n * tx; i += blockDim.x) {
         const int z = i / tx, c = i - z * tx;
         if (c < ncol) work[base + z * zstride + c] = res[i];
@@ -80,7 +81,8 @@ __global__ void __launch_bounds__(256) shell_ypass_kernel(typename cplx_t<T>::ty
                                                           int64_t d2hi, int ntx_active, RadixPlan plan) {
     using C = typename cplx_t<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int nh = n / 2 + 1, tx = tile_x<T>();
+    const int nh = n / 2 + 1;
+    constexpr int tx = tile_x<T>();
     const int z = blockIdx.x / ntx_active;
     const int x0 = (blockIdx.x % ntx_active) * tx;
     C* tw = reinterpret_cast<C*>(smem_raw);
@@ -98,7 +100,7 @@ __global__ void __launch_bounds__(256) shell_ypass_kernel(typename cplx_t<T>::ty
         buf0[i] = v;
     }
     __syncthreads();
-    C* res = fft_tile<T>(buf0, buf1, tw, plan, tx, tx, 1, true, -1);
+    C* res = fft_tile<T, tx>(buf0, buf1, tw, plan, tx, -1);
     for (int i = threadIdx.x; i < n * tx; i += blockDim.x) {
         const int y = i / tx, c = i - y * tx;
         if (c < ncol) work[base + (int64_t)y * nh + c] = res[i];
@@ -140,7 +142,7 @@ __global__ void __launch_bounds__(256) shell_xpass_kernel(const typename cplx_t<
         buf0[rr * h + k] = mk<T>(e.x - o.y, e.y + o.x);   // e + i*o
     }
     __syncthreads();
-    C* res = fft_tile<T>(buf0, buf1, twH, plan_half, nr, 1, h, false, -1);
+    C* res = fft_tile<T, 0>(buf0, buf1, twH, plan_half, nr, -1);
     double acc = 0.0;
     T local = 0;
     C* out = reinterpret_cast<C*>(field + r0 * n);

@@ -103,7 +103,7 @@ def _bk_oracle_subset(xyz, L, n, step, ncut, nmax, tri_idx):
     return np.array(out), p0k, nk
 
 
-@pytest.mark.parametrize("method", ["fp32"])
+@pytest.mark.parametrize("method", ["fp32", "bf16x3"])
 def test_bk_periodic_matches_oracle(method):
     """Bk_periodic end to end on uniform particles (N=48, step 2, Nmax 12)."""
     n, L, step, ncut, nmax = 48, 1000.0, 2, 2, 12
@@ -118,7 +118,7 @@ def test_bk_periodic_matches_oracle(method):
     bsum = plan.bsum.cpu().numpy()[idx]
     # raw triangle sums: error normalised by sum |F_i F_j F_l|
     err = np.abs(bsum - ref[:, 0]) / ref[:, 1]
-    assert err.max() < 1e-5, err.max()
+    assert err.max() < (1e-5 if method == "fp32" else 3e-5), err.max()
     # API values: recompute the reference formulas from the oracle sums
     nbar = xyz.shape[1] / L ** 3
     kf = 2 * np.pi / L
@@ -131,6 +131,6 @@ def test_bk_periodic_matches_oracle(method):
     # so the subtracted values are small differences of large numbers
     np.testing.assert_allclose(bk["p0k1"] + 1 / nbar, pp[:, 0] + 1 / nbar, rtol=1e-5)
     np.testing.assert_allclose(bk["b123_sn"], bsn, rtol=1e-5)
-    np.testing.assert_allclose(bk["b123"] + bk["b123_sn"], b + bsn, rtol=1e-5,
-                               atol=1e-5 * np.abs(b + bsn).max())
+    rt = 1e-5 if method == "fp32" else 1e-4
+    np.testing.assert_allclose(bk["b123"] + bk["b123_sn"], b + bsn, rtol=rt, atol=rt * np.abs(b + bsn).max())
     assert bk["meta"]["Ngrid"] == n and len(bk["b123"]) == len(idx)
