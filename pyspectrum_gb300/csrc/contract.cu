@@ -436,7 +436,7 @@ static int64_t loop_triangles(int jmin, int nmax) {
 static size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
 
 struct CountsLayout {
-    size_t work, field, dom, vox, wts, part, bsum, tri, total;
+    size_t work, tw, field, dom, vox, wts, part, bsum, tri, total;
 };
 
 
@@ -448,6 +448,7 @@ static CountsLayout counts_layout(int n, int step, int jmin, int nmax) {
     const int64_t nt = loop_triangles(jmin, nmax);
     size_t o = 0;
     L.work = o; o += al(shell_workspace_bytes<double>(n, 1));
+    L.tw = o; o += al((size_t)(n + n / 2) * sizeof(double2));
     L.field = o; o += al((size_t)V * sizeof(double));
     L.dom = o; o += al((size_t)nshell * nd * sizeof(double));
     L.vox = o; o += al((size_t)nd * sizeof(int64_t));
@@ -539,11 +540,13 @@ extern "C" int pyspec_bk_counts(int ngrid, int step, int jmin, int nmax, const i
     build_domain_kernel<<<(unsigned)((m * m * m + 255) / 256), 256, 0, st>>>(n, vox, wts);
     PYSPEC_LAUNCH_CHECK();
     count_launch();
+    double* part = reinterpret_cast<double*>(w + L.work + al((size_t)(n / 2 + 1) * n * n * sizeof(double2)));
+    double2* tw = reinterpret_cast<double2*>(w + L.tw);
+    PYSPEC_TRY(shell_twiddles<double>(tw, n, st));
     for (int s = 0; s < nshell; ++s) {
         // the x pass writes one partial per CTA right after the work grid
-        double* part = reinterpret_cast<double*>(w + L.work + al((size_t)(n / 2 + 1) * n * n * sizeof(double2)));
         PYSPEC_TRY((shell_one_impl<double, true>(nullptr, n, step, jmin + s, field, part,
-                                                  reinterpret_cast<double2*>(w + L.work), st)));
+                                                  reinterpret_cast<double2*>(w + L.work), tw, st)));
         gather_kernel<<<(unsigned)((nd + 255) / 256), 256, 0, st>>>(field, vox, nd, dom + (int64_t)s * nd);
         PYSPEC_LAUNCH_CHECK();
         count_launch();

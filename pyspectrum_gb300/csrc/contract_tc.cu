@@ -9,11 +9,11 @@
 // tensor memory (TMEM).
 //
 // CTA layout (1 CTA per SM, persistent over a contiguous voxel range):
-//   warps 0-14 (480 threads): producers.  Per chunk of KC = 32 voxels they
+//   warps 0-18 (608 threads): producers.  Per chunk of KC = 32 voxels they
 //     copy the fields in with cp.async, form the pair products, split both
 //     operands into hi/lo bf16 and store them in shared memory in the UMMA
 //     K-major core-matrix layout; then signal `full[stage]`.
-//   warp 15, lane 0: issues tcgen05.mma for the chunk and tcgen05.commit to
+//   warp 19, lane 0: issues tcgen05.mma for the chunk and tcgen05.commit to
 //     `empty[stage]` (frees the stage when the MMAs have read it).
 //   Every SEG chunks the accumulators are drained: the MMA thread commits to
 //   `seg`, the producers copy TMEM to a Kahan-compensated float32 sum per
@@ -39,7 +39,7 @@ constexpr int KC = 32;               // voxels per chunk (two k-steps of 16)
 constexpr int MAXROWS = 512;         // pair rows per CTA group (4 M-tiles)
 constexpr int MAXB = 64;             // shell rows of the B operand
 constexpr int NSTAGE = 2;
-constexpr int NPROD = 480;           // producer threads (warps 0-14); 16 warps in all -> 128 registers
+constexpr int NPROD = 608;           // producer threads (warps 0-18); 20 warps in all -> 96 registers
 constexpr int PWARPS = NPROD / 32;
 constexpr int UMAX = (4 * MAXROWS + NPROD - 1) / NPROD;   // A-operand units per producer thread
 constexpr int NTHREADS = NPROD + 32; // + the MMA warp
@@ -186,6 +186,18 @@ __device__ __forceinline__ void tmem_st16(uint32_t addr, const uint32_t* v) {
         : "memory");
 }
 
+__device__ __forceinline__ void tmem_ld8(uint32_t addr, uint32_t* v) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+                 : "r"(addr));
+}
+__device__ __forceinline__ void tmem_st8(uint32_t addr, const uint32_t* v) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};"
+                 :: "r"(addr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]),
+                    "r"(v[7])
+                 : "memory");
+}
+
 // TMEM columns of a group with C accumulator columns:
 //   [0, C)   MMA accumulators of the current segment
 //   [C, 2C)  running float32 sums (Kahan)        [2C, 3C) their compensation
@@ -239,17 +251,18 @@ __global__ void __launch_bounds__(NTHREADS, 1) contract_tc_kernel(const __grid_c
     const int q = warp & 3;                          // TMEM lane quarter of this warp
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
     const int nq = (PWARPS - q + 3) / 4;             // producer warps sharing this lane quarter
-    const int cstride = 16 * nq;                     // they take 16-column blocks round-robin
+    const int cstride = 8 * nq;                      // they take 8-column blocks round-robin
+    const int cfirst = 8 * (warp >> 2);
 
     if (warp < PWARPS) {
         // running sums start at zero
         {
-            uint32_t z[16];
+            uint32_t z[8];
 #pragma unroll
-            for (int e = 0; e < 16; ++e) z[e] = 0u;
-            for (int cb = 16 * (warp >> 2); cb < C; cb += cstride) {
-                tmem_st16(lane_base + (uint32_t)(C + cb), z);
-                tmem_st16(lane_base + (uint32_t)(2 * C + cb), z);
+            for (int e = 0; e < 8; ++e) z[e] = 0u;
+            for (int cb = cfirst; cb < C; cb += cstride) {
+                tmem_st8(lane_base + (uint32_t)(C + cb), z);
+                tmem_st8(lane_base + (uint32_t)(2 * C + cb), z);
             }
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         }
@@ -360,22 +373,22 @@ __global__ void __launch_bounds__(NTHREADS, 1) contract_tc_kernel(const __grid_c
                     continue;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                for (int cb = 16 * (warp >> 2); cb < C; cb += cstride) {
-                    uint32_t d[16], h[16], l[16];
-                    tmem_ld16(lane_base + (uint32_t)cb, d);
-                    tmem_ld16(lane_base + (uint32_t)(C + cb), h);
-                    tmem_ld16(lane_base + (uint32_t)(2 * C + cb), l);
+                for (int cb = cfirst; cb < C; cb += cstride) {
+                    uint32_t d[8], h[8], l[8];
+                    tmem_ld8(lane_base + (uint32_t)cb, d);
+                    tmem_ld8(lane_base + (uint32_t)(C + cb), h);
+                    tmem_ld8(lane_base + (uint32_t)(2 * C + cb), l);
                     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-                    for (int e = 0; e < 16; ++e) {
+                    for (int e = 0; e < 8; ++e) {
                         const float hs = __uint_as_float(h[e]), cs = __uint_as_float(l[e]);
                         const float y = __uint_as_float(d[e]) - cs;
                         const float t = hs + y;
                         l[e] = __float_as_uint((t - hs) - y);
                         h[e] = __float_as_uint(t);
                     }
-                    tmem_st16(lane_base + (uint32_t)(C + cb), h);
-                    tmem_st16(lane_base + (uint32_t)(2 * C + cb), l);
+                    tmem_st8(lane_base + (uint32_t)(C + cb), h);
+                    tmem_st8(lane_base + (uint32_t)(2 * C + cb), l);
                 }
                 asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -388,10 +401,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) contract_tc_kernel(const __grid_c
         // partial sums of this CTA: lane -> pair row, column -> shell slot
         if (!abort_flag) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            for (int cb = 16 * (warp >> 2); cb < C; cb += cstride) {
-                uint32_t h[16], l[16];
-                tmem_ld16(lane_base + (uint32_t)(C + cb), h);
-                tmem_ld16(lane_base + (uint32_t)(2 * C + cb), l);
+            for (int cb = cfirst; cb < C; cb += cstride) {
+                uint32_t h[8], l[8];
+                tmem_ld8(lane_base + (uint32_t)(C + cb), h);
+                tmem_ld8(lane_base + (uint32_t)(2 * C + cb), l);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                 int t = 0;
                 while (t + 1 < G.ntiles && cb >= G.tile_col[t + 1]) ++t;
@@ -401,7 +414,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) contract_tc_kernel(const __grid_c
                 const int row = 128 * t + 32 * q + lane;
                 const bool row_ok = row < rows;
 #pragma unroll
-                for (int e = 0; e < 16; ++e) {
+                for (int e = 0; e < 8; ++e) {
                     const int col = cb - G.tile_col[t] + e;
                     const int tri = row_ok ? P.tri_of[((size_t)G.table_off + row) * MAXB + col] : -1;
                     if (tri >= 0)

@@ -35,10 +35,25 @@ __host__ __device__ inline int64_t shell_d2hi(int j, int step) {
 
 __device__ __forceinline__ int fold(int i, int n) { return i <= n - i ? i : n - i; }
 
+// Twiddle tables for the forward (sign -1) transforms of one call, computed
+// once into the workspace: exp(-2 pi i m/n) for m < n, then exp(-2 pi i m/(n/2)).
+template <typename T>
+__global__ void twiddle_table_kernel(typename cplx_t<T>::type* tab, int n) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    fill_twiddles<T>(tab, n, -1, t, gridDim.x * blockDim.x);
+    fill_twiddles<T>(tab + n, n / 2, -1, t, gridDim.x * blockDim.x);
+}
+
+template <typename C>
+__device__ __forceinline__ void copy_table(C* dst, const C* __restrict__ src, int m) {
+    for (int i = threadIdx.x; i < m; i += blockDim.x) dst[i] = src[i];
+}
+
 template <typename T, bool INDICATOR>
 __global__ void __launch_bounds__(256) shell_zpass_kernel(const typename cplx_t<T>::type* __restrict__ half,
                                                           typename cplx_t<T>::type* __restrict__ work, int n,
-                                                          int64_t d2lo, int64_t d2hi, RadixPlan plan) {
+                                                          int64_t d2lo, int64_t d2hi, RadixPlan plan,
+                                                          const typename cplx_t<T>::type* __restrict__ twg) {
     using C = typename cplx_t<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nh = n / 2 + 1;
@@ -51,7 +66,7 @@ __global__ void __launch_bounds__(256) shell_zpass_kernel(const typename cplx_t<
     C* tw = reinterpret_cast<C*>(smem_raw);
     C* buf0 = tw + n;
     C* buf1 = buf0 + (size_t)tx * n;
-    fill_twiddles<T>(tw, n, -1, threadIdx.x, blockDim.x);
+    copy_table(tw, twg, n);
     const int ncol = min(tx, nh - x0);
     const int64_t zstride = (int64_t)n * nh;
     const int64_t base = (int64_t)y * nh + x0;
@@ -78,7 +93,8 @@ __global__ void __launch_bounds__(256) shell_zpass_kernel(const typename cplx_t<
 
 template <typename T>
 __global__ void __launch_bounds__(256) shell_ypass_kernel(typename cplx_t<T>::type* __restrict__ work, int n,
-                                                          int64_t d2hi, int ntx_active, RadixPlan plan) {
+                                                          int64_t d2hi, int ntx_active, RadixPlan plan,
+                                                          const typename cplx_t<T>::type* __restrict__ twg) {
     using C = typename cplx_t<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nh = n / 2 + 1;
@@ -88,7 +104,7 @@ __global__ void __launch_bounds__(256) shell_ypass_kernel(typename cplx_t<T>::ty
     C* tw = reinterpret_cast<C*>(smem_raw);
     C* buf0 = tw + n;
     C* buf1 = buf0 + (size_t)tx * n;
-    fill_twiddles<T>(tw, n, -1, threadIdx.x, blockDim.x);
+    copy_table(tw, twg, n);
     const int ncol = min(tx, nh - x0);
     const int64_t base = (int64_t)z * n * nh + x0;
     for (int i = threadIdx.x; i < n * tx; i += blockDim.x) {
@@ -107,11 +123,13 @@ __global__ void __launch_bounds__(256) shell_ypass_kernel(typename cplx_t<T>::ty
     }
 }
 
-// x rows: RL consecutive rows r = z*n + y per CTA.
+// x rows: RL consecutive rows r = z*n + y per CTA; warp w stages and packs
+// rows w, w+8, ... so no index needs a division.
 template <typename T>
 __global__ void __launch_bounds__(256) shell_xpass_kernel(const typename cplx_t<T>::type* __restrict__ work, int n,
                                                           int xlim, int rl, RadixPlan plan_half,
-                                                          T* __restrict__ field, double* __restrict__ part) {
+                                                          T* __restrict__ field, double* __restrict__ part,
+                                                          const typename cplx_t<T>::type* __restrict__ twg) {
     using C = typename cplx_t<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nh = n / 2 + 1, h = n / 2;
@@ -121,29 +139,31 @@ __global__ void __launch_bounds__(256) shell_xpass_kernel(const typename cplx_t<
     C* buf0 = stage + (size_t)rl * nh;         // rl * h
     C* buf1 = buf0 + (size_t)rl * h;
     __shared__ double red[32];
-    fill_twiddles<T>(twN, n, -1, threadIdx.x, blockDim.x);
-    fill_twiddles<T>(twH, h, -1, threadIdx.x, blockDim.x);
+    copy_table(twN, twg, n + h);               // both tables are contiguous
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
     const int64_t nrows = (int64_t)n * n;
     const int64_t r0 = (int64_t)blockIdx.x * rl;
     const int nr = (int)min((int64_t)rl, nrows - r0);
-    for (int i = threadIdx.x; i < nr * nh; i += blockDim.x) {
-        const int rr = i / nh, x = i - rr * nh;
-        stage[i] = x < xlim ? work[(r0 + rr) * nh + x] : mk<T>(0, 0);
+    for (int rr = warp; rr < nr; rr += nwarp) {
+        const C* src = work + (r0 + rr) * nh;
+        C* dst = stage + rr * nh;
+        for (int x = lane; x < nh; x += 32) dst[x] = x < xlim ? src[x] : mk<T>(0, 0);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < nr * h; i += blockDim.x) {
-        const int rr = i / h, k = i - rr * h;
+    for (int rr = warp; rr < nr; rr += nwarp) {
         const C* X = stage + rr * nh;
-        C a = X[k], b = X[h - k];
-        if (k == 0) { a.y = 0; b.y = 0; }
-        const C bc = mk<T>(b.x, -b.y);
-        const C e = cadd(a, bc);
-        const C o = cmul(csub(a, bc), twN[k]);
-        buf0[rr * h + k] = mk<T>(e.x - o.y, e.y + o.x);   // e + i*o
+        C* out = buf0 + rr * h;
+        for (int k = lane; k < h; k += 32) {
+            C a = X[k], b = X[h - k];
+            if (k == 0) { a.y = 0; b.y = 0; }
+            const C bc = mk<T>(b.x, -b.y);
+            const C e = cadd(a, bc);
+            const C o = cmul(csub(a, bc), twN[k]);
+            out[k] = mk<T>(e.x - o.y, e.y + o.x);   // e + i*o
+        }
     }
     __syncthreads();
     C* res = fft_tile<T, 0>(buf0, buf1, twH, plan_half, nr, -1);
-    double acc = 0.0;
     T local = 0;
     C* out = reinterpret_cast<C*>(field + r0 * n);
     for (int i = threadIdx.x; i < nr * h; i += blockDim.x) {
@@ -151,13 +171,13 @@ __global__ void __launch_bounds__(256) shell_xpass_kernel(const typename cplx_t<
         out[i] = v;       // f[2m] = Re z[m], f[2m+1] = Im z[m]; rows are contiguous
         local += v.x * v.x + v.y * v.y;
     }
-    acc = (double)local;
+    double acc = (double)local;
     // block reduction
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    if (lane == 0) red[warp] = acc;
     __syncthreads();
     if (threadIdx.x < 32) {
-        double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+        double v = threadIdx.x < nwarp ? red[threadIdx.x] : 0.0;
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (threadIdx.x == 0) part[blockIdx.x] = v;
     }
@@ -190,12 +210,14 @@ size_t shell_workspace_bytes(int n, int nshell) {
     size_t b = nh * n * n * sizeof(C);
     b = (b + 255) & ~(size_t)255;
     b += (size_t)nshell * nblk * sizeof(double);
+    b = (b + 255) & ~(size_t)255;
+    b += (size_t)(n + n / 2) * sizeof(C);          // twiddle tables
     return b;
 }
 
 template <typename T, bool INDICATOR>
 int shell_one_impl(const typename cplx_t<T>::type* half, int n, int step, int j, T* field, double* part,
-                   typename cplx_t<T>::type* work, cudaStream_t st) {
+                   typename cplx_t<T>::type* work, const typename cplx_t<T>::type* tw, cudaStream_t st) {
     using C = typename cplx_t<T>::type;
     RadixPlan plan, plan_half;
     PYSPEC_CHECK_ARG(n % 2 == 0 && make_plan(n, &plan) && make_plan(n / 2, &plan_half),
@@ -211,20 +233,29 @@ int shell_one_impl(const typename cplx_t<T>::type* half, int n, int step, int j,
     const size_t sm_zy = sizeof(C) * ((size_t)n + 2 * (size_t)tx * n);
     PYSPEC_TRY(allow_smem((const void*)shell_zpass_kernel<T, INDICATOR>, sm_zy));
     PYSPEC_TRY(allow_smem((const void*)shell_ypass_kernel<T>, sm_zy));
-    shell_zpass_kernel<T, INDICATOR><<<(unsigned)(ntx * n), 256, sm_zy, st>>>(half, work, n, d2lo, d2hi, plan);
+    shell_zpass_kernel<T, INDICATOR><<<(unsigned)(ntx * n), 256, sm_zy, st>>>(half, work, n, d2lo, d2hi, plan, tw);
     PYSPEC_LAUNCH_CHECK();
-    shell_ypass_kernel<T><<<(unsigned)(ntx_active * n), 256, sm_zy, st>>>(work, n, d2hi, ntx_active, plan);
+    shell_ypass_kernel<T><<<(unsigned)(ntx_active * n), 256, sm_zy, st>>>(work, n, d2hi, ntx_active, plan, tw);
     PYSPEC_LAUNCH_CHECK();
     const int rl = xpass_rows(n);
     const int h = n / 2;
     const size_t sm_x = sizeof(C) * ((size_t)n + h + (size_t)rl * nh + 2 * (size_t)rl * h);
     PYSPEC_TRY(allow_smem((const void*)shell_xpass_kernel<T>, sm_x));
     const unsigned nblk = (unsigned)(((int64_t)n * n + rl - 1) / rl);
-    shell_xpass_kernel<T><<<nblk, 256, sm_x, st>>>(work, n, xlim, rl, plan_half, field, part);
+    shell_xpass_kernel<T><<<nblk, 256, sm_x, st>>>(work, n, xlim, rl, plan_half, field, part, tw);
     PYSPEC_LAUNCH_CHECK();
     count_launch(3);
     return PYSPEC_OK;
 }
+
+template <typename T>
+int shell_twiddles(typename cplx_t<T>::type* tw, int n, cudaStream_t st) {
+    twiddle_table_kernel<T><<<4, 256, 0, st>>>(tw, n);
+    PYSPEC_LAUNCH_CHECK();
+    count_launch();
+    return PYSPEC_OK;
+}
+template int shell_twiddles<double>(double2*, int, cudaStream_t);
 
 template <typename T, bool INDICATOR>
 int shell_fields_impl(const typename cplx_t<T>::type* half, int n, int step, int jmin, int nmax, T* fields,
@@ -244,9 +275,13 @@ int shell_fields_impl(const typename cplx_t<T>::type* half, int n, int step, int
     const int rl = xpass_rows(n);
     const int nblk = (int)(((int64_t)n * n + rl - 1) / rl);
     const int64_t V = (int64_t)n * n * n;
+    off += (size_t)nshell * nblk * sizeof(double);
+    off = (off + 255) & ~(size_t)255;
+    C* tw = reinterpret_cast<C*>(reinterpret_cast<char*>(ws) + off);
+    PYSPEC_TRY(shell_twiddles<T>(tw, n, st));
     for (int s = 0; s < nshell; ++s) {
         PYSPEC_TRY((shell_one_impl<T, INDICATOR>(half, n, step, jmin + s, fields + (int64_t)s * V,
-                                                  part + (int64_t)s * nblk, work, st)));
+                                                  part + (int64_t)s * nblk, work, tw, st)));
     }
     if (p0sum) {
         reduce_rows_kernel<<<nshell, 256, 0, st>>>(part, nblk, p0sum);
@@ -263,7 +298,7 @@ template int shell_fields_impl<float, false>(const float2*, int, int, int, int, 
 template int shell_fields_impl<double, true>(const double2*, int, int, int, int, double*, double*, void*,
                                              size_t, cudaStream_t);
 template int shell_one_impl<double, true>(const double2*, int, int, int, double*, double*, double2*,
-                                          cudaStream_t);
+                                          const double2*, cudaStream_t);
 
 // Nk[j] for j = 0..nmax over the full grid (pyspectrum.py:380)
 __global__ void mode_counts_kernel(int n, int step, int nmax, unsigned long long* __restrict__ nk) {

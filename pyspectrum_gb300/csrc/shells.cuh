@@ -22,7 +22,11 @@ int shell_fields_impl(const typename cplx_t<T>::type* half, int n, int step, int
 
 template <typename T, bool INDICATOR>
 int shell_one_impl(const typename cplx_t<T>::type* half, int n, int step, int j, T* field, double* part,
-                   typename cplx_t<T>::type* work, cudaStream_t st);
+                   typename cplx_t<T>::type* work, const typename cplx_t<T>::type* tw, cudaStream_t st);
+
+// fills the forward twiddle tables used by shell_one_impl: n + n/2 values
+template <typename T>
+int shell_twiddles(typename cplx_t<T>::type* tw, int n, cudaStream_t st);
 
 int mode_counts_impl(int n, int step, int nmax, int64_t* nk, cudaStream_t st);
 
