@@ -151,6 +151,28 @@ int pyspec_bk_contract(const float *fields, int ngrid, int nshell, const int32_t
                        void *workspace, size_t ws_bytes, void *stream);
 
 /* ------------------------------------------------------------------------
+ * Triangle contraction without device allocation.  This entry point has no
+ * counterpart in the reference.  It is for callers that cannot allocate
+ * device memory where they run -- inside another framework's
+ * foreign-function / custom-call hook that hands over only the operands, or
+ * while a stream is being captured.  It computes what pyspec_bk_contract
+ * computes with PYSPEC_CONTRACT_FP32 (same kernel, same sums), with its
+ * scratch in a fixed device array of PYSPEC_NOALLOC_SCRATCH_BYTES that the
+ * library holds on every GPU that loads it until the process exits.
+ *  - Requests whose scratch would exceed that size (roughly ntri x 152 CTAs
+ *    x 8 bytes of partial sums plus the tile tables) return PYSPEC_E_INVALID.
+ *  - No call allocates device memory (it copies its tile tables from host
+ *    memory into the array and clears the partial sums it uses).
+ *  - All calls share the one array: calls whose work overlaps on the GPU race
+ *    and must be ordered by the caller.
+ *  - The first call on a device looks up the array's address with that
+ *    device current; make it before any stream capture.
+ * ---------------------------------------------------------------------- */
+#define PYSPEC_NOALLOC_SCRATCH_BYTES (16u << 20)
+int pyspec_bk_contract_noalloc(const float *fields, int ngrid, int nshell,
+                               const int32_t *tri_host, int ntri, double *bsum, void *stream);
+
+/* ------------------------------------------------------------------------
  * Triangle counts -- pyspectrum.py:962-1030 (_counts_Bk123) and
  * estimator.f:2-102 (bk_counts): counts[t] = round(sum_x I_i I_j I_l / N^3),
  * I_j = FFT of the shell-j indicator, evaluated in float64 and returned as
