@@ -12,12 +12,13 @@ namespace pyspec {
 
 // Pass over contiguous lines (the x axis): lines [line0, line0+nl) of length n
 // occupy one contiguous run of memory.
-template <typename T>
+template <typename T, int NC>
 __global__ void __launch_bounds__(256) fft_contig_kernel(typename cplx_t<T>::type* data, int64_t nlines_total,
-                                                         int lx, RadixPlan plan, int sign) {
+                                                         int lx_rt, RadixPlan plan, int sign) {
     using C = typename cplx_t<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int n = plan.n;
+    const int n = NC > 0 ? NC : plan.n;
+    const int lx = NC > 0 ? contig_lines(NC) : lx_rt;
     C* tw = reinterpret_cast<C*>(smem_raw);
     C* buf0 = tw + n;
     C* buf1 = buf0 + (size_t)lx * n;
@@ -28,20 +29,22 @@ __global__ void __launch_bounds__(256) fft_contig_kernel(typename cplx_t<T>::typ
     const int cnt = nl * n;
     for (int i = threadIdx.x; i < cnt; i += blockDim.x) buf0[i] = g[i];
     __syncthreads();
-    C* res = fft_tile<T, 0>(buf0, buf1, tw, plan, nl, sign);
+    C* res;
+    if constexpr (NC > 0) res = ct::fft_tile_ct<T, NC, 0, contig_lines(NC)>(buf0, buf1, tw, sign);
+    else res = fft_tile<T, 0>(buf0, buf1, tw, plan, nl, sign);
     for (int i = threadIdx.x; i < cnt; i += blockDim.x) g[i] = res[i];
 }
 
 // Pass over strided lines: a tile is `tx` consecutive x columns x all n
 // positions along the transformed axis (row stride `row_stride` elements).
 // Tile b covers outer index b / ntx and x block b % ntx.
-template <typename T>
+template <typename T, int NC>
 __global__ void __launch_bounds__(256) fft_strided_kernel(typename cplx_t<T>::type* data, int nx, int64_t row_stride,
                                                           int64_t outer_stride, RadixPlan plan, int sign) {
     using C = typename cplx_t<T>::type;
     constexpr int tx = tile_x<T>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int n = plan.n;
+    const int n = NC > 0 ? NC : plan.n;
     C* tw = reinterpret_cast<C*>(smem_raw);
     C* buf0 = tw + n;
     C* buf1 = buf0 + (size_t)tx * n;
@@ -57,7 +60,9 @@ __global__ void __launch_bounds__(256) fft_strided_kernel(typename cplx_t<T>::ty
         if (c < ncol) buf0[i] = g[r * row_stride + c];
     }
     __syncthreads();
-    C* res = fft_tile<T, tx>(buf0, buf1, tw, plan, tx, sign);
+    C* res;
+    if constexpr (NC > 0) res = ct::fft_tile_ct<T, NC, tx, 0>(buf0, buf1, tw, sign);
+    else res = fft_tile<T, tx>(buf0, buf1, tw, plan, tx, sign);
     for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
         const int r = i / tx, c = i - r * tx;
         if (c < ncol) g[r * row_stride + c] = res[i];
@@ -70,27 +75,38 @@ int fft3d_c2c_impl(typename cplx_t<T>::type* data, int n, int sign, cudaStream_t
     RadixPlan plan;
     PYSPEC_CHECK_ARG(make_plan(n, &plan), "ngrid=%d must factor into 2, 3 and 5", n);
     PYSPEC_CHECK_ARG(sign == 1 || sign == -1, "sign must be +1 or -1");
-    // x lines
-    {
-        int lx = max(1, min(16, 4096 / n));
-        size_t sm = sizeof(C) * ((size_t)n + 2 * (size_t)lx * n);
-        PYSPEC_TRY(allow_smem((const void*)fft_contig_kernel<T>, sm));
-        int64_t lines = (int64_t)n * n;
-        unsigned nb = (unsigned)((lines + lx - 1) / lx);
-        fft_contig_kernel<T><<<nb, 256, sm, st>>>(data, lines, lx, plan, sign);
-        PYSPEC_LAUNCH_CHECK();
-        count_launch();
-    }
-    // y and z lines
+    const int lx = contig_lines(n);
+    const size_t sm_c = sizeof(C) * ((size_t)n + 2 * (size_t)lx * n);
+    const int64_t lines = (int64_t)n * n;
+    const unsigned nbc = (unsigned)((lines + lx - 1) / lx);
     const int tx = tile_x<T>();
     const int ntx = (n + tx - 1) / tx;
-    size_t sm = sizeof(C) * ((size_t)n + 2 * (size_t)tx * n);
-    PYSPEC_TRY(allow_smem((const void*)fft_strided_kernel<T>, sm));
-    fft_strided_kernel<T><<<(unsigned)(ntx * n), 256, sm, st>>>(data, n, n, (int64_t)n * n, plan, sign);
-    PYSPEC_LAUNCH_CHECK();
-    fft_strided_kernel<T><<<(unsigned)(ntx * n), 256, sm, st>>>(data, n, (int64_t)n * n, n, plan, sign);
-    PYSPEC_LAUNCH_CHECK();
-    count_launch(2);
+    const size_t sm = sizeof(C) * ((size_t)n + 2 * (size_t)tx * n);
+#define PYSPEC_FFT3D_LAUNCH(NCV)                                                                          \
+    do {                                                                                                 \
+        PYSPEC_TRY(allow_smem((const void*)fft_contig_kernel<T, NCV>, sm_c));                            \
+        PYSPEC_TRY(allow_smem((const void*)fft_strided_kernel<T, NCV>, sm));                             \
+        fft_contig_kernel<T, NCV><<<nbc, 256, sm_c, st>>>(data, lines, lx, plan, sign);                  \
+        PYSPEC_LAUNCH_CHECK();                                                                           \
+        fft_strided_kernel<T, NCV><<<(unsigned)(ntx * n), 256, sm, st>>>(data, n, n, (int64_t)n * n, plan, sign); \
+        PYSPEC_LAUNCH_CHECK();                                                                           \
+        fft_strided_kernel<T, NCV><<<(unsigned)(ntx * n), 256, sm, st>>>(data, n, (int64_t)n * n, n, plan, sign); \
+        PYSPEC_LAUNCH_CHECK();                                                                           \
+    } while (0)
+    bool done = false;
+    if constexpr (sizeof(T) == 4) {
+        done = true;
+        switch (n) {
+            case 192: PYSPEC_FFT3D_LAUNCH(192); break;
+            case 256: PYSPEC_FFT3D_LAUNCH(256); break;
+            case 360: PYSPEC_FFT3D_LAUNCH(360); break;
+            case 512: PYSPEC_FFT3D_LAUNCH(512); break;
+            default: done = false;
+        }
+    }
+    if (!done) PYSPEC_FFT3D_LAUNCH(0);
+#undef PYSPEC_FFT3D_LAUNCH
+    count_launch(3);
     return PYSPEC_OK;
 }
 

@@ -191,3 +191,95 @@ __device__ typename cplx_t<T>::type* fft_tile(typename cplx_t<T>::type* buf0, ty
 }
 
 }  // namespace pyspec
+
+// ---------------------------------------------------------------------------
+// Compile-time plans.  For the line lengths the estimator uses most (the
+// grid sizes 96..512 and their halves) the radices, strides and loop trip
+// counts are template constants, so every index is a constant multiply/shift
+// and each stage's loop is fully unrolled.
+// ---------------------------------------------------------------------------
+namespace pyspec {
+namespace ct {
+
+constexpr int kRadices[5] = {8, 4, 5, 3, 2};
+
+constexpr int nstages(int n) {
+    int m = n, s = 0;
+    for (int k = 0; k < 5; ++k)
+        while (m % kRadices[k] == 0) { m /= kRadices[k]; ++s; }
+    return m == 1 ? s : -1;
+}
+constexpr int radix_at(int n, int stage) {
+    int m = n, s = 0;
+    for (int k = 0; k < 5; ++k)
+        while (m % kRadices[k] == 0) {
+            if (s == stage) return kRadices[k];
+            m /= kRadices[k];
+            ++s;
+        }
+    return 0;
+}
+constexpr int ns_at(int n, int stage) {
+    int p = 1;
+    for (int s = 0; s < stage; ++s) p *= radix_at(n, s);
+    return p;
+}
+
+template <typename T, int N, int LINES, int NL, int S>
+__device__ __forceinline__ typename cplx_t<T>::type* stages(typename cplx_t<T>::type* __restrict__ src,
+                                                           typename cplx_t<T>::type* __restrict__ dst,
+                                                           const typename cplx_t<T>::type* __restrict__ tw,
+                                                           int sign) {
+    using C = typename cplx_t<T>::type;
+    if constexpr (S >= nstages(N)) {
+        return src;
+    } else {
+        constexpr int R = radix_at(N, S);
+        constexpr int Ns = ns_at(N, S);
+        constexpr int nb = N / R;
+        constexpr int twstep = nb / Ns;
+        constexpr int nlines = LINES > 0 ? LINES : NL;
+        constexpr int items = nb * nlines;
+        constexpr int es = LINES > 0 ? LINES : 1;
+        constexpr int ls = LINES > 0 ? 1 : N;
+        for (int it = threadIdx.x; it < items; it += blockDim.x) {
+            int j, line;
+            if constexpr (LINES > 0) { line = it % LINES; j = it / LINES; }
+            else { line = it / nb; j = it - line * nb; }
+            const C* s = src + line * ls;
+            C v[R];
+            const int jb = j / Ns;
+            const int k = j - jb * Ns;
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[r] = s[(j + r * nb) * es];
+            if constexpr (Ns > 1) {
+#pragma unroll
+                for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * k * twstep]);
+            }
+            if constexpr (R == 2) dft2<T>(v);
+            else if constexpr (R == 3) dft3<T>(v, sign);
+            else if constexpr (R == 4) dft4<T>(v, sign);
+            else if constexpr (R == 5) dft5<T>(v, sign);
+            else dft8<T>(v, sign);
+            C* d = dst + line * ls;
+            const int base = jb * Ns * R + k;
+#pragma unroll
+            for (int r = 0; r < R; ++r) d[(base + r * Ns) * es] = v[r];
+        }
+        __syncthreads();
+        return stages<T, N, LINES, NL, S + 1>(dst, src, tw, sign);
+    }
+}
+
+// Same contract as fft_tile<T, LINES>, for a line length N and (when
+// LINES == 0) a line count NL known at compile time.
+template <typename T, int N, int LINES, int NL>
+__device__ __forceinline__ typename cplx_t<T>::type* fft_tile_ct(typename cplx_t<T>::type* buf0,
+                                                                typename cplx_t<T>::type* buf1,
+                                                                const typename cplx_t<T>::type* tw, int sign) {
+    static_assert(nstages(N) > 0, "line length must factor into 2, 3 and 5");
+    return stages<T, N, LINES, NL, 0>(buf0, buf1, tw, sign);
+}
+
+}  // namespace ct
+}  // namespace pyspec

@@ -17,6 +17,7 @@
 // with X[0] and X[N/2] replaced by their real parts -- this equals
 // Re(sum over the full grid) for any half grid, which is what the reference's
 // np.real(fftn(...)) computes.
+#include <algorithm>
 #include "fft_device.cuh"
 #include "fft3d.cuh"
 #include "shells.cuh"
@@ -35,6 +36,11 @@ __host__ __device__ inline int64_t shell_d2hi(int j, int step) {
 
 __device__ __forceinline__ int fold(int i, int n) { return i <= n - i ? i : n - i; }
 
+// rows of the x pass handled by one CTA
+__host__ __device__ constexpr int xpass_rows_ct(int n) {
+    return (4096 / n) < 1 ? 1 : ((4096 / n) > 16 ? 16 : 4096 / n);
+}
+
 // Twiddle tables for the forward (sign -1) transforms of one call, computed
 // once into the workspace: exp(-2 pi i m/n) for m < n, then exp(-2 pi i m/(n/2)).
 template <typename T>
@@ -49,13 +55,14 @@ __device__ __forceinline__ void copy_table(C* dst, const C* __restrict__ src, in
     for (int i = threadIdx.x; i < m; i += blockDim.x) dst[i] = src[i];
 }
 
-template <typename T, bool INDICATOR>
+template <typename T, bool INDICATOR, int NC>
 __global__ void __launch_bounds__(256) shell_zpass_kernel(const typename cplx_t<T>::type* __restrict__ half,
-                                                          typename cplx_t<T>::type* __restrict__ work, int n,
+                                                          typename cplx_t<T>::type* __restrict__ work, int n_rt,
                                                           int64_t d2lo, int64_t d2hi, RadixPlan plan,
                                                           const typename cplx_t<T>::type* __restrict__ twg) {
     using C = typename cplx_t<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n = NC > 0 ? NC : n_rt;
     const int nh = n / 2 + 1;
     constexpr int tx = tile_x<T>();
     const int ntx = (nh + tx - 1) / tx;
@@ -84,19 +91,22 @@ __global__ void __launch_bounds__(256) shell_zpass_kernel(const typename cplx_t<
         buf0[i] = v;
     }
     __syncthreads();
-    C* res = fft_tile<T, tx>(buf0, buf1, tw, plan, tx, -1);
+    C* res;
+    if constexpr (NC > 0) res = ct::fft_tile_ct<T, NC, tx, 0>(buf0, buf1, tw, -1);
+    else res = fft_tile<T, tx>(buf0, buf1, tw, plan, tx, -1);
     for (int i = threadIdx.x; i < n * tx; i += blockDim.x) {
         const int z = i / tx, c = i - z * tx;
         if (c < ncol) work[base + z * zstride + c] = res[i];
     }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) shell_ypass_kernel(typename cplx_t<T>::type* __restrict__ work, int n,
+template <typename T, int NC>
+__global__ void __launch_bounds__(256) shell_ypass_kernel(typename cplx_t<T>::type* __restrict__ work, int n_rt,
                                                           int64_t d2hi, int ntx_active, RadixPlan plan,
                                                           const typename cplx_t<T>::type* __restrict__ twg) {
     using C = typename cplx_t<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n = NC > 0 ? NC : n_rt;
     const int nh = n / 2 + 1;
     constexpr int tx = tile_x<T>();
     const int z = blockIdx.x / ntx_active;
@@ -116,63 +126,99 @@ __global__ void __launch_bounds__(256) shell_ypass_kernel(typename cplx_t<T>::ty
         buf0[i] = v;
     }
     __syncthreads();
-    C* res = fft_tile<T, tx>(buf0, buf1, tw, plan, tx, -1);
+    C* res;
+    if constexpr (NC > 0) res = ct::fft_tile_ct<T, NC, tx, 0>(buf0, buf1, tw, -1);
+    else res = fft_tile<T, tx>(buf0, buf1, tw, plan, tx, -1);
     for (int i = threadIdx.x; i < n * tx; i += blockDim.x) {
         const int y = i / tx, c = i - y * tx;
         if (c < ncol) work[base + (int64_t)y * nh + c] = res[i];
     }
 }
 
-// x rows: RL consecutive rows r = z*n + y per CTA; warp w stages and packs
-// rows w, w+8, ... so no index needs a division.
-template <typename T>
-__global__ void __launch_bounds__(256) shell_xpass_kernel(const typename cplx_t<T>::type* __restrict__ work, int n,
-                                                          int xlim, int rl, RadixPlan plan_half,
+// Asynchronous copy of one complex element (8 or 16 bytes); bytes = 0 zero-fills.
+template <typename C>
+__device__ __forceinline__ void cp_async_elem(uint32_t dst, const void* src, int bytes) {
+    if constexpr (sizeof(C) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" :: "r"(dst), "l"(src), "r"(bytes) : "memory");
+    else
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" :: "r"(dst), "l"(src), "r"(bytes) : "memory");
+}
+
+// x rows: a persistent CTA walks blocks of RL consecutive rows r = z*n + y.
+// The rows of the next block are copied into the other staging buffer with
+// cp.async while the current block is transformed, so the loads are always in
+// flight.  Warp w stages and packs rows w, w+8, ... (no divisions).
+template <typename T, int NC>
+__global__ void __launch_bounds__(256) shell_xpass_kernel(const typename cplx_t<T>::type* __restrict__ work, int n_rt,
+                                                          int xlim, int rl_rt, RadixPlan plan_half,
                                                           T* __restrict__ field, double* __restrict__ part,
                                                           const typename cplx_t<T>::type* __restrict__ twg) {
     using C = typename cplx_t<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n = NC > 0 ? NC : n_rt;
+    const int rl = NC > 0 ? xpass_rows_ct(NC) : rl_rt;
     const int nh = n / 2 + 1, h = n / 2;
     C* twN = reinterpret_cast<C*>(smem_raw);   // exp(-2 pi i m / n), m < n
     C* twH = twN + n;                          // exp(-2 pi i m / (n/2))
-    C* stage = twH + h;                        // rl * nh
-    C* buf0 = stage + (size_t)rl * nh;         // rl * h
+    C* stage0 = twH + h;                       // 2 x rl * nh
+    C* buf0 = stage0 + 2 * (size_t)rl * nh;    // rl * h
     C* buf1 = buf0 + (size_t)rl * h;
     __shared__ double red[32];
     copy_table(twN, twg, n + h);               // both tables are contiguous
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
     const int64_t nrows = (int64_t)n * n;
-    const int64_t r0 = (int64_t)blockIdx.x * rl;
-    const int nr = (int)min((int64_t)rl, nrows - r0);
-    for (int rr = warp; rr < nr; rr += nwarp) {
-        const C* src = work + (r0 + rr) * nh;
-        C* dst = stage + rr * nh;
-        for (int x = lane; x < nh; x += 32) dst[x] = x < xlim ? src[x] : mk<T>(0, 0);
-    }
-    __syncthreads();
-    for (int rr = warp; rr < nr; rr += nwarp) {
-        const C* X = stage + rr * nh;
-        C* out = buf0 + rr * h;
-        for (int k = lane; k < h; k += 32) {
-            C a = X[k], b = X[h - k];
-            if (k == 0) { a.y = 0; b.y = 0; }
-            const C bc = mk<T>(b.x, -b.y);
-            const C e = cadd(a, bc);
-            const C o = cmul(csub(a, bc), twN[k]);
-            out[k] = mk<T>(e.x - o.y, e.y + o.x);   // e + i*o
+    const int64_t nblocks = (nrows + rl - 1) / rl;
+    auto issue = [&](int64_t blk, int sbuf) {
+        if (blk < nblocks) {
+            const int64_t r0 = blk * rl;
+            const int nr = (int)min((int64_t)rl, nrows - r0);
+            C* st = stage0 + (size_t)sbuf * rl * nh;
+            for (int rr = warp; rr < nr; rr += nwarp) {
+                const C* src = work + (r0 + rr) * nh;
+                const uint32_t dst = (uint32_t)__cvta_generic_to_shared(st + rr * nh);
+                for (int x = lane; x < nh; x += 32)
+                    cp_async_elem<C>(dst + (uint32_t)(x * sizeof(C)), x < xlim ? (const void*)(src + x) : (const void*)src,
+                                     x < xlim ? (int)sizeof(C) : 0);
+            }
         }
-    }
-    __syncthreads();
-    C* res = fft_tile<T, 0>(buf0, buf1, twH, plan_half, nr, -1);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
     T local = 0;
-    C* out = reinterpret_cast<C*>(field + r0 * n);
-    for (int i = threadIdx.x; i < nr * h; i += blockDim.x) {
-        const C v = res[i];
-        out[i] = v;       // f[2m] = Re z[m], f[2m+1] = Im z[m]; rows are contiguous
-        local += v.x * v.x + v.y * v.y;
+    int sb = 0;
+    issue(blockIdx.x, 0);
+    for (int64_t blk = blockIdx.x; blk < nblocks; blk += gridDim.x, sb ^= 1) {
+        issue(blk + gridDim.x, sb ^ 1);
+        asm volatile("cp.async.wait_group 1;" ::: "memory");
+        __syncthreads();
+        const int64_t r0 = blk * rl;
+        const int nr = (int)min((int64_t)rl, nrows - r0);
+        const C* st = stage0 + (size_t)sb * rl * nh;
+        for (int rr = warp; rr < nr; rr += nwarp) {
+            const C* X = st + rr * nh;
+            C* out = buf0 + rr * h;
+            for (int k = lane; k < h; k += 32) {
+                C a = X[k], b = X[h - k];
+                if (k == 0) { a.y = 0; b.y = 0; }
+                const C bc = mk<T>(b.x, -b.y);
+                const C e = cadd(a, bc);
+                const C o = cmul(csub(a, bc), twN[k]);
+                out[k] = mk<T>(e.x - o.y, e.y + o.x);   // e + i*o
+            }
+        }
+        __syncthreads();
+        C* res;
+        if constexpr (NC > 0) res = ct::fft_tile_ct<T, NC / 2, 0, xpass_rows_ct(NC)>(buf0, buf1, twH, -1);
+        else res = fft_tile<T, 0>(buf0, buf1, twH, plan_half, nr, -1);
+        C* out = reinterpret_cast<C*>(field + r0 * n);
+        for (int i = threadIdx.x; i < nr * h; i += blockDim.x) {
+            const C v = res[i];
+            out[i] = v;       // f[2m] = Re z[m], f[2m+1] = Im z[m]; rows are contiguous
+            local += v.x * v.x + v.y * v.y;
+        }
+        __syncthreads();      // buffers are rewritten by the next block
     }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
     double acc = (double)local;
-    // block reduction
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) red[warp] = acc;
     __syncthreads();
@@ -199,14 +245,21 @@ __global__ void reduce_rows_kernel(const double* __restrict__ part, int nper, do
     }
 }
 
-static int xpass_rows(int n) { return max(1, min(16, 4096 / n)); }
+static int xpass_rows(int n) { return xpass_rows_ct(n); }
+
+// persistent x-pass CTAs: a few per SM, never more than there are row blocks
+static int xpass_ctas(int n) {
+    int sms = 152, dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t blocks = ((int64_t)n * n + xpass_rows(n) - 1) / xpass_rows(n);
+    return (int)std::min<int64_t>(blocks, (int64_t)sms * 3);
+}
 
 template <typename T>
 size_t shell_workspace_bytes(int n, int nshell) {
     using C = typename cplx_t<T>::type;
     const size_t nh = n / 2 + 1;
-    const int rl = xpass_rows(n);
-    const size_t nblk = ((size_t)n * n + rl - 1) / rl;
+    const size_t nblk = (size_t)xpass_ctas(n);
     size_t b = nh * n * n * sizeof(C);
     b = (b + 255) & ~(size_t)255;
     b += (size_t)nshell * nblk * sizeof(double);
@@ -231,19 +284,38 @@ int shell_one_impl(const typename cplx_t<T>::type* half, int n, int step, int j,
     const int ntx_active = min(ntx, kmax / tx + 1);
     const int xlim = min(nh, ntx_active * tx);
     const size_t sm_zy = sizeof(C) * ((size_t)n + 2 * (size_t)tx * n);
-    PYSPEC_TRY(allow_smem((const void*)shell_zpass_kernel<T, INDICATOR>, sm_zy));
-    PYSPEC_TRY(allow_smem((const void*)shell_ypass_kernel<T>, sm_zy));
-    shell_zpass_kernel<T, INDICATOR><<<(unsigned)(ntx * n), 256, sm_zy, st>>>(half, work, n, d2lo, d2hi, plan, tw);
-    PYSPEC_LAUNCH_CHECK();
-    shell_ypass_kernel<T><<<(unsigned)(ntx_active * n), 256, sm_zy, st>>>(work, n, d2hi, ntx_active, plan, tw);
-    PYSPEC_LAUNCH_CHECK();
     const int rl = xpass_rows(n);
     const int h = n / 2;
-    const size_t sm_x = sizeof(C) * ((size_t)n + h + (size_t)rl * nh + 2 * (size_t)rl * h);
-    PYSPEC_TRY(allow_smem((const void*)shell_xpass_kernel<T>, sm_x));
-    const unsigned nblk = (unsigned)(((int64_t)n * n + rl - 1) / rl);
-    shell_xpass_kernel<T><<<nblk, 256, sm_x, st>>>(work, n, xlim, rl, plan_half, field, part, tw);
-    PYSPEC_LAUNCH_CHECK();
+    const size_t sm_x = sizeof(C) * ((size_t)n + h + 2 * (size_t)rl * nh + 2 * (size_t)rl * h);
+    const unsigned nblk = (unsigned)xpass_ctas(n);
+    // compile-time plans for the common grid sizes (single precision)
+#define PYSPEC_SHELL_LAUNCH(NCV)                                                                          \
+    do {                                                                                                 \
+        PYSPEC_TRY(allow_smem((const void*)shell_zpass_kernel<T, INDICATOR, NCV>, sm_zy));               \
+        PYSPEC_TRY(allow_smem((const void*)shell_ypass_kernel<T, NCV>, sm_zy));                          \
+        PYSPEC_TRY(allow_smem((const void*)shell_xpass_kernel<T, NCV>, sm_x));                           \
+        shell_zpass_kernel<T, INDICATOR, NCV><<<(unsigned)(ntx * n), 256, sm_zy, st>>>(half, work, n, d2lo, \
+                                                                                         d2hi, plan, tw);   \
+        PYSPEC_LAUNCH_CHECK();                                                                           \
+        shell_ypass_kernel<T, NCV><<<(unsigned)(ntx_active * n), 256, sm_zy, st>>>(work, n, d2hi,         \
+                                                                                   ntx_active, plan, tw); \
+        PYSPEC_LAUNCH_CHECK();                                                                           \
+        shell_xpass_kernel<T, NCV><<<nblk, 256, sm_x, st>>>(work, n, xlim, rl, plan_half, field, part, tw); \
+        PYSPEC_LAUNCH_CHECK();                                                                           \
+    } while (0)
+    bool done = false;
+    if constexpr (sizeof(T) == 4) {
+        done = true;
+        switch (n) {
+            case 192: PYSPEC_SHELL_LAUNCH(192); break;
+            case 256: PYSPEC_SHELL_LAUNCH(256); break;
+            case 360: PYSPEC_SHELL_LAUNCH(360); break;
+            case 512: PYSPEC_SHELL_LAUNCH(512); break;
+            default: done = false;
+        }
+    }
+    if (!done) PYSPEC_SHELL_LAUNCH(0);
+#undef PYSPEC_SHELL_LAUNCH
     count_launch(3);
     return PYSPEC_OK;
 }
@@ -272,8 +344,7 @@ int shell_fields_impl(const typename cplx_t<T>::type* half, int n, int step, int
     const size_t nh = n / 2 + 1;
     size_t off = (nh * n * n * sizeof(C) + 255) & ~(size_t)255;
     double* part = reinterpret_cast<double*>(reinterpret_cast<char*>(ws) + off);
-    const int rl = xpass_rows(n);
-    const int nblk = (int)(((int64_t)n * n + rl - 1) / rl);
+    const int nblk = xpass_ctas(n);
     const int64_t V = (int64_t)n * n * n;
     off += (size_t)nshell * nblk * sizeof(double);
     off = (off + 255) & ~(size_t)255;

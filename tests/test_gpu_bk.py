@@ -48,6 +48,29 @@ def test_shell_fields_match_oracle(n, step, jmin, nmax):
         np.testing.assert_allclose(p0g[s], np.sum(F[j] ** 2), rtol=1e-5)
 
 
+@pytest.mark.parametrize("n,step,shells", [(192, 3, (1, 17, 40)), (256, 4, (2, 31))])
+def test_shell_fields_large_grids(n, step, shells):
+    """Grid sizes with compile-time FFT plans, checked against numpy on a few shells."""
+    rng = np.random.default_rng(n)
+    half = (rng.standard_normal((n // 2 + 1, n, n)) + 1j * rng.standard_normal((n // 2 + 1, n, n))) / n ** 1.5
+    half[0] = half[0].real
+    df = O.reflect_delta(half, n)
+    irk = O.shell_index(n, step)
+    jmin, nmax = min(shells), max(shells)
+    S = nmax - jmin + 1
+    h = torch.from_numpy(_zyx(half.astype(np.complex64))).cuda()
+    fields = torch.empty((S, n ** 3), dtype=torch.float32, device="cuda")
+    p0 = torch.empty(S, dtype=torch.float64, device="cuda")
+    ws = torch.empty(core._lib.load().pyspec_shell_fields_workspace(n, S), dtype=torch.uint8, device="cuda")
+    call("pyspec_shell_fields", ptr(h), n, step, jmin, nmax, ptr(fields), ptr(p0), ptr(ws), ws.numel(), stream_ptr())
+    for j in shells:
+        ref = np.real(np.fft.fftn(np.where(irk == j, df, 0))).transpose(2, 1, 0)
+        got = fields[j - jmin].cpu().numpy().reshape(n, n, n)
+        scale = np.abs(ref).max()
+        assert np.abs(got - ref).max() < 3e-6 * scale, (j, np.abs(got - ref).max() / scale)
+        np.testing.assert_allclose(p0[j - jmin].item(), np.sum(ref.astype(np.float64) ** 2), rtol=1e-5)
+
+
 @pytest.mark.parametrize("n,step,ncut,nmax", [(16, 1, 1, 8), (16, 3, 3, 5), (24, 2, 2, 6), (32, 3, 3, 5)])
 def test_counts_match_reference_compute_path(golden, n, step, ncut, nmax):
     g = golden("ref_bk_small.npz")

@@ -14,7 +14,7 @@ def _zyx(a_xyz):
     return np.ascontiguousarray(np.asarray(a_xyz).transpose(2, 1, 0))
 
 
-@pytest.mark.parametrize("n", [8, 16, 24, 30, 40, 64, 96])
+@pytest.mark.parametrize("n", [8, 16, 24, 30, 40, 64, 96, 192, 256])
 @pytest.mark.parametrize("sign", [1, -1])
 def test_fft3d_c2c_matches_numpy(n, sign):
     rng = np.random.default_rng(n)
@@ -25,6 +25,23 @@ def test_fft3d_c2c_matches_numpy(n, sign):
     ref = np.fft.fftn(a.astype(np.complex128)) if sign < 0 else np.fft.ifftn(a.astype(np.complex128)) * n ** 3
     err = np.abs(got - ref).max() / np.abs(ref).max()
     assert err < 2e-6, err
+
+
+@pytest.mark.parametrize("n", [360, 512])
+def test_fft3d_roundtrip_large(n):
+    """Forward then backward transform returns N^3 times the input (sizes with
+    compile-time plans), and Parseval holds."""
+    g = torch.Generator(device="cuda").manual_seed(n)
+    a = torch.complex(torch.randn((n, n, n), device="cuda", generator=g),
+                      torch.randn((n, n, n), device="cuda", generator=g))
+    t = a.clone()
+    call("pyspec_fft3d_c2c", ptr(t), n, -1, stream_ptr())
+    e_k = (t.abs() ** 2).double().sum().item()
+    call("pyspec_fft3d_c2c", ptr(t), n, 1, stream_ptr())
+    err = ((t / float(n) ** 3 - a).abs().max() / a.abs().max()).item()
+    assert err < 2e-6, err
+    e_x = (a.abs() ** 2).double().sum().item()
+    assert abs(e_k / float(n) ** 3 - e_x) / e_x < 1e-5
 
 
 def test_fft_matches_reference_golden(golden):
