@@ -9,17 +9,22 @@
 // tensor memory (TMEM).
 //
 // CTA layout (1 CTA per SM, persistent over a contiguous voxel range):
-//   warps 0-18 (608 threads): producers.  Per chunk of KC = 32 voxels they
-//     copy the fields in with cp.async, form the pair products, split both
-//     operands into hi/lo bf16 and store them in shared memory in the UMMA
-//     K-major core-matrix layout; then signal `full[stage]`.
-//   warp 19, lane 0: issues tcgen05.mma for the chunk and tcgen05.commit to
-//     `empty[stage]` (frees the stage when the MMAs have read it).
+//   warps 0-15 (512 threads): producers.  Warp w owns TMEM lane quarter w%4
+//     of pair tile w/4: lane l is pair row 128*(w/4) + 32*(w%4) + l.  Per
+//     chunk of KC = 32 voxels the fields arrive in shared memory by cp.async
+//     (prefetched 3 chunks ahead); each thread forms its pair's products,
+//     splits them into hi/lo bf16 and writes them straight into TMEM
+//     (tcgen05.st) as the MMA's A operand; the B operand (the shells' hi/lo
+//     parts) goes to shared memory in the UMMA K-major core-matrix layout.
+//     Then `full[stage]` is signalled.
+//   warp 16, lane 0: issues tcgen05.mma (A from TMEM, B from shared memory)
+//     and tcgen05.commit to `empty[stage]`.
 //   Every SEG chunks the accumulators are drained: the MMA thread commits to
-//   `seg`, the producers copy TMEM to a Kahan-compensated float32 sum per
-//   triangle in shared memory and arrive on `drained`; the next MMA restarts
-//   the accumulators.  At the end each CTA writes one float64 partial per
-//   triangle; a second kernel adds the partials in a fixed order.
+//   `seg`, the producers add the TMEM accumulators into Kahan-compensated
+//   float32 sums per triangle in shared memory and arrive on `drained`; the
+//   next MMA restarts the accumulators.  At the end each CTA writes one float64
+//   partial per triangle; a second kernel adds the partials in a fixed order.
+// TMEM columns: [0, C) accumulators; then two A stages of 32 columns per tile.
 // Every mbarrier wait is bounded; on timeout the kernel records an error
 // code, stops issuing work, waits (bounded) for its MMAs in flight, frees its
 // TMEM and returns.
@@ -39,22 +44,22 @@ constexpr int KC = 32;               // voxels per chunk (two k-steps of 16)
 constexpr int MAXROWS = 512;         // pair rows per CTA group (4 M-tiles)
 constexpr int MAXB = 64;             // shell rows of the B operand
 constexpr int NSTAGE = 2;
-constexpr int NPROD = 608;           // producer threads (warps 0-18); 20 warps in all -> 96 registers
+constexpr int NPROD = 512;           // producer threads (warps 0-15): 4 tiles x 4 TMEM lane quarters
 constexpr int PWARPS = NPROD / 32;
-constexpr int UMAX = (4 * MAXROWS + NPROD - 1) / NPROD;   // A-operand units per producer thread
 constexpr int NTHREADS = NPROD + 32; // + the MMA warp
 constexpr int SEG = 64;              // chunks between accumulator drains
 constexpr int FSTRIDE = KC + 4;      // padded float row of the field staging buffer
 constexpr int MAXGROUPS = 8;
 constexpr int MAXTILES = 4;
-constexpr int MAXCOLS = 160;         // accumulator columns per group: 3 x 160 <= 512 TMEM columns
-constexpr int NFBUF = 4;             // field staging buffers (prefetch distance NFBUF-1 chunks)
+constexpr int MAXCOLS = 256;         // accumulator columns per group (+ 2 x 4 x 32 A columns <= 512)
+constexpr int ACOLS = 32;            // TMEM columns of one tile's A operand per stage (2 k-steps x (8 hi + 8 lo))
+constexpr int NFBUF = 8;             // field staging buffers (prefetch distance NFBUF-1 chunks)
 constexpr unsigned long long kWaitNs = 2000000000ull;   // 2 s bound on any mbarrier wait
 
-constexpr int A_BYTES = MAXROWS * KC * 2;      // one of hi / lo
-constexpr int B_BYTES = MAXB * KC * 2;
-constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
-constexpr int F_BYTES = MAXB * FSTRIDE * 4;
+constexpr int B_BYTES = MAXB * KC * 2;         // one of hi / lo
+constexpr int STAGE_BYTES = 2 * B_BYTES;
+// one staging buffer holds the nshell field rows of a chunk
+__host__ __device__ constexpr int f_bytes(int nshell) { return (nshell * FSTRIDE * 4 + 127) / 128 * 128; }
 
 struct Group {
     int rows;              // pair rows used (<= 512)
@@ -62,7 +67,8 @@ struct Group {
     int tile_n[MAXTILES];  // N of each tile (multiple of 16)
     int tile_col[MAXTILES];// TMEM column offset of each tile
     int ncols;             // TMEM columns allocated (power of 2 >= 32)
-    int table_off;         // offset of this group in the row / triangle tables
+    int table_off;         // offset of this group in the row / slot tables
+    int nslots;            // triangles (Kahan slots) of this group
 };
 
 struct Params {
@@ -74,10 +80,12 @@ struct Params {
     int64_t nchunks;
     int64_t chunks_per_cta;
     const int16_t* pair_ij;      // [group][512][2] shell slots (-1 for padding rows)
-    const int32_t* tri_of;       // [group][512][MAXB] triangle index of (pair row, shell) or -1
+    const int32_t* slot_of;      // [group][512][MAXB] accumulator slot of (pair row, shell) or -1
+    const int32_t* slot_tri;     // [group][maxslots] triangle index of each slot
     double* partials;            // [gridDim.x][ntri]
     int* err;
     int ngroups;
+    int maxslots;
     Group g[MAXGROUPS];
 };
 
@@ -91,20 +99,20 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
     return t;
 }
 
-// Waits for the mbarrier phase with the given parity.  The thread sleeps in
-// try_wait (suspend-time hint 0.5 ms) instead of spinning; the wait gives up
-// after kWaitNs and returns false.
+// Waits for the mbarrier phase with the given parity by polling try_wait
+// (no suspend hint: a sleeping thread wakes too late for a per-chunk
+// handshake); the wait gives up after kWaitNs and returns false.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     uint32_t ok;
     asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
                  : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
     if (ok) return true;
     const unsigned long long t0 = globaltimer_ns();
-    while (true) {
-        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\nselp.u32 %0, 1, 0, p;\n}\n"
-                     : "=r"(ok) : "r"(bar), "r"(parity), "r"(500000u) : "memory");
+    for (uint32_t it = 1;; ++it) {
+        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
         if (ok) return true;
-        if (globaltimer_ns() - t0 > kWaitNs) return false;
+        if ((it & 255u) == 0 && globaltimer_ns() - t0 > kWaitNs) return false;
     }
 }
 
@@ -198,9 +206,6 @@ __device__ __forceinline__ void tmem_st8(uint32_t addr, const uint32_t* v) {
                  : "memory");
 }
 
-// TMEM columns of a group with C accumulator columns:
-//   [0, C)   MMA accumulators of the current segment
-//   [C, 2C)  running float32 sums (Kahan)        [2C, 3C) their compensation
 __global__ void __launch_bounds__(NTHREADS, 1) contract_tc_kernel(const __grid_constant__ Params P) {
     extern __shared__ __align__(1024) unsigned char smem[];
     // this CTA's group descriptor, copied out of parameter space once (a
@@ -208,8 +213,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) contract_tc_kernel(const __grid_c
     __shared__ Group G;
     if (threadIdx.x == 0) G = P.g[blockIdx.y];
     __syncthreads();
-    unsigned char* stage_base = smem;                                   // NSTAGE * STAGE_BYTES
-    float* fbuf = reinterpret_cast<float*>(smem + NSTAGE * STAGE_BYTES);  // NFBUF x F_BYTES
+    unsigned char* stage_base = smem;                                          // NSTAGE x (B hi, B lo)
+    float* fbuf = reinterpret_cast<float*>(smem + NSTAGE * STAGE_BYTES);       // NFBUF x F_BYTES
+    const int F_BYTES = f_bytes(P.nshell);
+    float2* acc = reinterpret_cast<float2*>(smem + NSTAGE * STAGE_BYTES + NFBUF * F_BYTES);  // Kahan (sum, comp)
     __shared__ __align__(8) uint64_t bar_full[NSTAGE], bar_empty[NSTAGE], bar_seg, bar_drained;
     __shared__ uint32_t tmem_slot;
     __shared__ int16_t pij[MAXROWS * 2];
@@ -226,17 +233,18 @@ __global__ void __launch_bounds__(NTHREADS, 1) contract_tc_kernel(const __grid_c
 
     // ---- set-up ----
     for (int i = tid; i < MAXROWS * 2; i += NTHREADS) pij[i] = P.pair_ij[(size_t)G.table_off * 2 + i];
-    // zero both stages once: padding rows and padding shells stay zero
+    for (int i = tid; i < G.nslots; i += NTHREADS) acc[i] = make_float2(0.f, 0.f);
+    // zero both B stages once: padding shells stay zero
     for (int i = tid; i < NSTAGE * STAGE_BYTES / 16; i += NTHREADS)
         reinterpret_cast<uint4*>(stage_base)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
         abort_flag = 0;
         for (int s = 0; s < NSTAGE; ++s) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_full[s])), "r"(NPROD));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_full[s])), "r"(PWARPS));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_empty[s])), "r"(1));
         }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_seg)), "r"(1));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_drained)), "r"(NPROD));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_drained)), "r"(PWARPS));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == PWARPS) {
@@ -250,45 +258,19 @@ __global__ void __launch_bounds__(NTHREADS, 1) contract_tc_kernel(const __grid_c
     const uint32_t tmem = tmem_slot;
     const int q = warp & 3;                          // TMEM lane quarter of this warp
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
-    const int nq = (PWARPS - q + 3) / 4;             // producer warps sharing this lane quarter
-    const int cstride = 8 * nq;                      // they take 8-column blocks round-robin
-    const int cfirst = 8 * (warp >> 2);
+    // A operand of tile t, stage s, k-step ks: 8 hi columns then 8 lo columns
+    auto acol = [&](int s, int t, int ks) { return (uint32_t)(C + (s * MAXTILES + t) * ACOLS + ks * 16); };
 
     if (warp < PWARPS) {
-        // running sums start at zero
-        {
-            uint32_t z[8];
-#pragma unroll
-            for (int e = 0; e < 8; ++e) z[e] = 0u;
-            for (int cb = cfirst; cb < C; cb += cstride) {
-                tmem_st8(lane_base + (uint32_t)(C + cb), z);
-                tmem_st8(lane_base + (uint32_t)(2 * C + cb), z);
-            }
-            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-        }
         // ================= producers =================
         const int rows = G.rows;
         const int nsh = P.nshell;
-        // Every chunk has the same work units, so each thread resolves its
-        // shared-memory offsets once: A units (pair row r, 8-voxel group g),
-        // one B unit (shell r, group g), one 16-byte field copy.
-        int ua_fi[UMAX], ua_fj[UMAX], ua_off[UMAX];
-#pragma unroll
-        for (int k = 0; k < UMAX; ++k) {
-            const int u = tid + k * NPROD;
-            ua_off[k] = -1;
-            ua_fi[k] = ua_fj[k] = 0;
-            if (u < rows * 4) {
-                const int g = (u >= rows) + (u >= 2 * rows) + (u >= 3 * rows);
-                const int r = u - g * rows;
-                const int i = pij[2 * r], j = pij[2 * r + 1];
-                if (i >= 0) {
-                    ua_fi[k] = i * FSTRIDE + 8 * g;
-                    ua_fj[k] = j * FSTRIDE + 8 * g;
-                    ua_off[k] = op_off(r, g);
-                }
-            }
-        }
+        const int mytile = warp >> 2;                 // warp-uniform
+        const bool tile_on = mytile < G.ntiles;
+        const int row = 128 * mytile + 32 * q + lane;
+        const bool row_on = tile_on && row < rows && pij[2 * row] >= 0;
+        const int fi = row_on ? pij[2 * row] * FSTRIDE : 0;
+        const int fj = row_on ? pij[2 * row + 1] * FSTRIDE : 0;
         int ub_f = -1, ub_off = 0;
         if (tid < nsh * 4) {
             const int g = (tid >= nsh) + (tid >= 2 * nsh) + (tid >= 3 * nsh);
@@ -333,13 +315,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) contract_tc_kernel(const __grid_c
                     abort_flag = 1;
                     continue;
                 }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             }
             const float* F = fbuf + (size_t)(c % NFBUF) * (F_BYTES / 4);
-            char* st = reinterpret_cast<char*>(stage_base) + (size_t)s * STAGE_BYTES;
-            char* Ahi = st;
-            char* Alo = st + A_BYTES;
-            char* Bhi = st + 2 * A_BYTES;
-            char* Blo = st + 2 * A_BYTES + B_BYTES;
+            char* Bhi = reinterpret_cast<char*>(stage_base) + (size_t)s * STAGE_BYTES;
+            char* Blo = Bhi + B_BYTES;
             // B operand: shells 0..nshell-1 (rows >= nshell stay zero)
             if (ub_f >= 0) {
                 const float4 a = *reinterpret_cast<const float4*>(F + ub_f);
@@ -348,24 +328,42 @@ __global__ void __launch_bounds__(NTHREADS, 1) contract_tc_kernel(const __grid_c
                                      make_float2(b.z, b.w)};
                 split_store8(x, Bhi + ub_off, Blo + ub_off);
             }
-            // A operand: pair products
+            // A operand: this lane's pair products, straight into TMEM
+            if (tile_on) {
 #pragma unroll
-            for (int k = 0; k < UMAX; ++k) {
-                if (ua_off[k] < 0) continue;
-                const float4 a0 = *reinterpret_cast<const float4*>(F + ua_fi[k]);
-                const float4 a1 = *reinterpret_cast<const float4*>(F + ua_fi[k] + 4);
-                const float4 b0 = *reinterpret_cast<const float4*>(F + ua_fj[k]);
-                const float4 b1 = *reinterpret_cast<const float4*>(F + ua_fj[k] + 4);
-                const float2 x[4] = {mul2(make_float2(a0.x, a0.y), make_float2(b0.x, b0.y)),
-                                     mul2(make_float2(a0.z, a0.w), make_float2(b0.z, b0.w)),
-                                     mul2(make_float2(a1.x, a1.y), make_float2(b1.x, b1.y)),
-                                     mul2(make_float2(a1.z, a1.w), make_float2(b1.z, b1.w))};
-                split_store8(x, Ahi + ua_off[k], Alo + ua_off[k]);
+                for (int ks = 0; ks < KC / 16; ++ks) {
+                    uint32_t h[8], l[8];
+#pragma unroll
+                    for (int g = 0; g < 4; ++g) {
+                        float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+                        if (row_on) {
+                            a = *reinterpret_cast<const float4*>(F + fi + 16 * ks + 4 * g);
+                            b = *reinterpret_cast<const float4*>(F + fj + 16 * ks + 4 * g);
+                        }
+                        const float2 p0 = mul2(make_float2(a.x, a.y), make_float2(b.x, b.y));
+                        const float2 p1 = mul2(make_float2(a.z, a.w), make_float2(b.z, b.w));
+                        h[2 * g] = pack_bf16x2(p0.x, p0.y);
+                        h[2 * g + 1] = pack_bf16x2(p1.x, p1.y);
+                        const float2 l0 = sub2(p0, make_float2(__uint_as_float(h[2 * g] << 16),
+                                                               __uint_as_float(h[2 * g] & 0xFFFF0000u)));
+                        const float2 l1 = sub2(p1, make_float2(__uint_as_float(h[2 * g + 1] << 16),
+                                                               __uint_as_float(h[2 * g + 1] & 0xFFFF0000u)));
+                        l[2 * g] = pack_bf16x2(l0.x, l0.y);
+                        l[2 * g + 1] = pack_bf16x2(l1.x, l1.y);
+                    }
+                    tmem_st8(lane_base + acol(s, mytile, ks), h);
+                    tmem_st8(lane_base + acol(s, mytile, ks) + 8u, l);
+                }
+                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_arrive(smem_u32(&bar_full[s]));
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            // one arrive per warp (the barrier counts warps): the lanes' writes are
+            // ordered before lane 0's release by the warp barrier
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&bar_full[s]));
             // drain after the last chunk of every segment: add the segment's
-            // accumulators into the running Kahan sums, all inside TMEM
+            // accumulators into the Kahan sums in shared memory
             if ((c + 1) % SEG == 0 || c + 1 == nch) {
                 if (!mbar_wait(smem_u32(&bar_seg), seg_count & 1)) {
                     atomicExch(P.err, 2);
@@ -373,58 +371,39 @@ __global__ void __launch_bounds__(NTHREADS, 1) contract_tc_kernel(const __grid_c
                     continue;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                for (int cb = cfirst; cb < C; cb += cstride) {
-                    uint32_t d[8], h[8], l[8];
+                // the four warps of this lane quarter take 8-column blocks round-robin
+                for (int cb = 8 * (warp >> 2); cb < C; cb += 32) {
+                    uint32_t d[8];
                     tmem_ld8(lane_base + (uint32_t)cb, d);
-                    tmem_ld8(lane_base + (uint32_t)(C + cb), h);
-                    tmem_ld8(lane_base + (uint32_t)(2 * C + cb), l);
                     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    int t = 0;
+                    while (t + 1 < G.ntiles && cb >= G.tile_col[t + 1]) ++t;
+                    if (cb >= G.tile_col[t] + G.tile_n[t]) continue;
+                    const int drow = 128 * t + 32 * q + lane;
+                    const bool drow_ok = drow < rows;
 #pragma unroll
                     for (int e = 0; e < 8; ++e) {
-                        const float hs = __uint_as_float(h[e]), cs = __uint_as_float(l[e]);
-                        const float y = __uint_as_float(d[e]) - cs;
-                        const float t = hs + y;
-                        l[e] = __float_as_uint((t - hs) - y);
-                        h[e] = __float_as_uint(t);
+                        const int col = cb - G.tile_col[t] + e;
+                        const int slot = drow_ok ? P.slot_of[((size_t)G.table_off + drow) * MAXB + col] : -1;
+                        if (slot < 0) continue;
+                        const float2 a = acc[slot];
+                        const float y = __uint_as_float(d[e]) - a.y;
+                        const float sum = a.x + y;
+                        acc[slot] = make_float2(sum, (sum - a.x) - y);
                     }
-                    tmem_st8(lane_base + (uint32_t)(C + cb), h);
-                    tmem_st8(lane_base + (uint32_t)(2 * C + cb), l);
                 }
-                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-                mbar_arrive(smem_u32(&bar_drained));
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(&bar_drained));
                 ++seg_count;
             }
         }
 #undef PYSPEC_ISSUE_FIELDS
         asm volatile("cp.async.wait_group 0;" ::: "memory");
-        // partial sums of this CTA: lane -> pair row, column -> shell slot
-        if (!abort_flag) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            for (int cb = cfirst; cb < C; cb += cstride) {
-                uint32_t h[8], l[8];
-                tmem_ld8(lane_base + (uint32_t)(C + cb), h);
-                tmem_ld8(lane_base + (uint32_t)(2 * C + cb), l);
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                int t = 0;
-                while (t + 1 < G.ntiles && cb >= G.tile_col[t + 1]) ++t;
-                if (cb >= G.tile_col[t] + G.tile_n[t]) continue;
-                // no lane-dependent branch around the .sync.aligned TMEM loads:
-                // rows past the group's last pair are masked in the store
-                const int row = 128 * t + 32 * q + lane;
-                const bool row_ok = row < rows;
-#pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                    const int col = cb - G.tile_col[t] + e;
-                    const int tri = row_ok ? P.tri_of[((size_t)G.table_off + row) * MAXB + col] : -1;
-                    if (tri >= 0)
-                        P.partials[(size_t)blockIdx.x * P.ntri + tri] =
-                            (double)__uint_as_float(h[e]) - (double)__uint_as_float(l[e]);
-                }
-            }
-        }
     } else if (lane == 0) {
         // ================= MMA issuer =================
+        // Small-N MMAs are bound by their issue cost, so every operand address
+        // is computed once: B descriptors and A TMEM addresses per (stage, k-step).
         const int ntiles = G.ntiles;
         uint32_t idesc[MAXTILES], dcol[MAXTILES];
 #pragma unroll
@@ -433,36 +412,44 @@ __global__ void __launch_bounds__(NTHREADS, 1) contract_tc_kernel(const __grid_c
             dcol[t] = tmem + (uint32_t)G.tile_col[t];
         }
         const uint32_t sbase = smem_u32(stage_base);
+        uint64_t dbh[NSTAGE][KC / 16], dbl[NSTAGE][KC / 16];
+        uint32_t aad[NSTAGE][KC / 16][MAXTILES];
+#pragma unroll
+        for (int s = 0; s < NSTAGE; ++s)
+#pragma unroll
+            for (int ks = 0; ks < KC / 16; ++ks) {
+                const uint32_t bhi = sbase + (uint32_t)(s * STAGE_BYTES) + (uint32_t)(ks * 256);
+                dbh[s][ks] = make_desc(bhi, 128, 512);
+                dbl[s][ks] = make_desc(bhi + B_BYTES, 128, 512);
+#pragma unroll
+                for (int t = 0; t < MAXTILES; ++t) aad[s][ks][t] = tmem + acol(s, t, ks);
+            }
         int seg_count = 0;
-        bool fresh = true;   // next MMA of each tile overwrites the accumulator
+        uint32_t first = 0;   // 0: the next MMA of each tile overwrites its accumulator
         for (int c = 0; c < nch; ++c) {
             const int s = c & 1;
             if (!mbar_wait(smem_u32(&bar_full[s]), (c >> 1) & 1)) { atomicExch(P.err, 3); abort_flag = 1; break; }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t st = sbase + (uint32_t)(s * STAGE_BYTES);
-            const uint32_t ahi = st, alo = st + A_BYTES, bhi = st + 2 * A_BYTES, blo = st + 2 * A_BYTES + B_BYTES;
 #pragma unroll
             for (int ks = 0; ks < KC / 16; ++ks) {
-                const uint32_t koff = (uint32_t)(ks * 256);       // two core matrices along K
-                const uint64_t dbh = make_desc(bhi + koff, 128, 512);
-                const uint64_t dbl = make_desc(blo + koff, 128, 512);
+                const uint64_t bh = s ? dbh[1][ks] : dbh[0][ks];
+                const uint64_t bl = s ? dbl[1][ks] : dbl[0][ks];
+                const uint32_t acc0 = ks == 0 ? first : 1u;
 #pragma unroll
                 for (int t = 0; t < MAXTILES; ++t) {
-                    if (t >= ntiles) break;
-                    const uint32_t toff = (uint32_t)(t * 128 / 8 * 512);
-                    const uint64_t dah = make_desc(ahi + toff + koff, 128, 512);
-                    const uint64_t dal = make_desc(alo + toff + koff, 128, 512);
-                    const uint32_t d = dcol[t];
-                    const uint32_t first = (fresh && ks == 0) ? 0u : 1u;
-                    asm volatile("{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-                                 :: "r"(d), "l"(dah), "l"(dbh), "r"(idesc[t]), "r"(first));
-                    asm volatile("{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-                                 :: "r"(d), "l"(dah), "l"(dbl), "r"(idesc[t]), "r"(1u));
-                    asm volatile("{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-                                 :: "r"(d), "l"(dal), "l"(dbh), "r"(idesc[t]), "r"(1u));
+                    if (t < ntiles) {
+                        const uint32_t ahi = s ? aad[1][ks][t] : aad[0][ks][t];
+                        const uint32_t alo = ahi + 8u;
+                        asm volatile("{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n"
+                                     :: "r"(dcol[t]), "r"(ahi), "l"(bh), "r"(idesc[t]), "r"(acc0));
+                        asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, 1;"
+                                     :: "r"(dcol[t]), "r"(ahi), "l"(bl), "r"(idesc[t]));
+                        asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, 1;"
+                                     :: "r"(dcol[t]), "r"(alo), "l"(bh), "r"(idesc[t]));
+                    }
                 }
             }
-            fresh = false;
+            first = 1u;
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                          :: "r"(smem_u32(&bar_empty[s])) : "memory");
             if ((c + 1) % SEG == 0 || c + 1 == nch) {
@@ -471,7 +458,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) contract_tc_kernel(const __grid_c
                 if (!mbar_wait(smem_u32(&bar_drained), seg_count & 1)) { atomicExch(P.err, 4); abort_flag = 1; break; }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 ++seg_count;
-                fresh = true;
+                first = 0u;
             }
         }
         // make sure no MMA is still running before the TMEM is released
@@ -483,6 +470,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) contract_tc_kernel(const __grid_c
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
+    // partial sums of this CTA's triangles
+    if (!abort_flag) {
+        for (int i = tid; i < G.nslots; i += NTHREADS) {
+            const int t = P.slot_tri[(size_t)blockIdx.y * P.maxslots + i];
+            P.partials[(size_t)blockIdx.x * P.ntri + t] = (double)acc[i].x - (double)acc[i].y;
+        }
+    }
     if (warp == PWARPS) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(G.ncols));
@@ -497,7 +491,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) contract_tc_kernel(const __grid_c
 struct HostPlan {
     Params base;           // pointers filled at launch
     std::vector<int16_t> pair_ij;
-    std::vector<int32_t> tri_of;
+    std::vector<int32_t> slot_of;
+    std::vector<int32_t> slot_tri;
     size_t smem = 0;
     bool ok = false;
     char why[160] = {0};
@@ -537,29 +532,40 @@ static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri) {
         return x.second != y.second ? x.second < y.second : x.first < y.first;
     });
     const int nrows = (int)order.size();
-    // N of each 128-row tile: the largest shell column it needs, rounded to 16
-    std::vector<int> tile_n;
+    // N of each 128-row tile: the largest shell column it needs, rounded to 16;
+    // and the number of triangles (Kahan slots) it holds
+    std::vector<int> tile_n, tile_slots;
     for (int r0 = 0; r0 < nrows; r0 += 128) {
-        int maxl = 0;
-        for (int r = r0; r < std::min(nrows, r0 + 128); ++r)
+        int maxl = 0, ns = 0;
+        for (int r = r0; r < std::min(nrows, r0 + 128); ++r) {
             for (auto& lt : pairs[order[r]]) maxl = std::max(maxl, lt.first);
+            ns += (int)pairs[order[r]].size();
+        }
         tile_n.push_back(((maxl + 1) + 15) / 16 * 16);
+        tile_slots.push_back(ns);
     }
     const int ntiles_all = (int)tile_n.size();
-    // Greedy grouping: at most 4 tiles and MAXCOLS accumulator columns per CTA
-    // group (the group's TMEM holds 3 x its columns: MMA sums, Kahan sums and
-    // compensations).
+    const size_t fixed = (size_t)NSTAGE * STAGE_BYTES + (size_t)NFBUF * f_bytes(nshell);
+    const int budget = (int)((227 * 1024 - 4096 - fixed) / sizeof(float2));
+    // Greedy grouping into CTA groups: at most 4 tiles, MAXCOLS accumulator
+    // columns (TMEM also holds 2 stages x 4 tiles x 32 A columns) and `budget`
+    // Kahan slots in shared memory.
     std::vector<int> group_first;
     {
-        int cur_tiles = 0, cur_cols = 0;
+        int cur_tiles = 0, cur_cols = 0, cur_slots = 0;
         for (int t = 0; t < ntiles_all; ++t) {
-            if (cur_tiles == 0 || cur_tiles == MAXTILES || cur_cols + tile_n[t] > MAXCOLS) {
+            if (tile_slots[t] > budget) {
+                snprintf(hp->why, sizeof(hp->why), "a 128-row tile holds %d triangles (limit %d)", tile_slots[t], budget);
+                return hp;
+            }
+            if (cur_tiles == 0 || cur_tiles == MAXTILES || cur_cols + tile_n[t] > MAXCOLS ||
+                cur_slots + tile_slots[t] > budget) {
                 group_first.push_back(t);
-                cur_tiles = 0;
-                cur_cols = 0;
+                cur_tiles = cur_cols = cur_slots = 0;
             }
             ++cur_tiles;
             cur_cols += tile_n[t];
+            cur_slots += tile_slots[t];
         }
     }
     const int ngroups = (int)group_first.size();
@@ -572,7 +578,9 @@ static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri) {
     P.ntri = ntri;
     int nb = 16;
     hp->pair_ij.assign((size_t)ngroups * MAXROWS * 2, (int16_t)-1);
-    hp->tri_of.assign((size_t)ngroups * MAXROWS * MAXB, -1);
+    hp->slot_of.assign((size_t)ngroups * MAXROWS * MAXB, -1);
+    std::vector<std::vector<int32_t>> gslots(ngroups);
+    int maxslots = 1;
     for (int g = 0; g < ngroups; ++g) {
         Group& G = P.g[g];
         const int t0 = group_first[g];
@@ -589,7 +597,7 @@ static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri) {
             col += G.tile_n[t];
             nb = std::max(nb, G.tile_n[t]);
         }
-        G.ncols = pow2_cols(3 * col);
+        G.ncols = pow2_cols(col + NSTAGE * MAXTILES * ACOLS);
         if (G.ncols > 512) {
             snprintf(hp->why, sizeof(hp->why), "BF16x3 tile columns exceed TMEM");
             return hp;
@@ -598,15 +606,24 @@ static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri) {
             auto key = order[r0 + r];
             hp->pair_ij[((size_t)G.table_off + r) * 2] = (int16_t)key.first;
             hp->pair_ij[((size_t)G.table_off + r) * 2 + 1] = (int16_t)key.second;
-            for (auto& lt : pairs[key]) hp->tri_of[((size_t)G.table_off + r) * MAXB + lt.first] = lt.second;
+            for (auto& lt : pairs[key]) {
+                hp->slot_of[((size_t)G.table_off + r) * MAXB + lt.first] = (int32_t)gslots[g].size();
+                gslots[g].push_back(lt.second);
+            }
         }
+        G.nslots = (int)gslots[g].size();
+        maxslots = std::max(maxslots, G.nslots);
     }
     if (nb > MAXB) {
         snprintf(hp->why, sizeof(hp->why), "BF16x3 contraction supports at most %d shells", MAXB);
         return hp;
     }
     P.nb = nb;
-    hp->smem = (size_t)NSTAGE * STAGE_BYTES + (size_t)NFBUF * F_BYTES;
+    P.maxslots = maxslots;
+    hp->slot_tri.assign((size_t)ngroups * maxslots, 0);
+    for (int g = 0; g < ngroups; ++g)
+        for (size_t i = 0; i < gslots[g].size(); ++i) hp->slot_tri[(size_t)g * maxslots + i] = gslots[g][i];
+    hp->smem = fixed + sizeof(float2) * (size_t)maxslots;
     hp->ok = true;
     return hp;
 }
@@ -638,7 +655,7 @@ static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 size_t contract_tc_ws(int64_t nvox, int nshell, int ntri) {
     // tables (bounded by the largest plan for nshell <= 64) + partials + error word
     const size_t rows = (size_t)tc::MAXGROUPS * tc::MAXROWS;
-    const size_t tables = rows * 2 * 2 + rows * tc::MAXB * 4 + 4096;
+    const size_t tables = rows * 2 * 2 + rows * tc::MAXB * 4 + (size_t)tc::MAXGROUPS * (size_t)ntri * 4 + 4096;
     const int64_t nchunks = (nvox + tc::KC - 1) / tc::KC;
     const size_t gx = (size_t)std::min<int64_t>(std::max<int64_t>(nchunks, 1), 1024);
     return tc::al256(tables) + tc::al256(gx * (size_t)std::max(ntri, 1) * sizeof(double)) + 256;
@@ -664,7 +681,8 @@ int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_
     size_t off = 0;
     int* d_err = reinterpret_cast<int*>(w + off); off += 256;      // status word first
     int16_t* d_pair = reinterpret_cast<int16_t*>(w + off); off += al256(hp->pair_ij.size() * 2);
-    int32_t* d_tri = reinterpret_cast<int32_t*>(w + off); off += al256(hp->tri_of.size() * 4);
+    int32_t* d_slot = reinterpret_cast<int32_t*>(w + off); off += al256(hp->slot_of.size() * 4);
+    int32_t* d_stri = reinterpret_cast<int32_t*>(w + off); off += al256(hp->slot_tri.size() * 4);
     const int64_t nchunks = (nvox + KC - 1) / KC;
     const int gx = grid_x(nchunks, hp->base.ngroups);
     double* partials = reinterpret_cast<double*>(w + off);
@@ -673,7 +691,8 @@ int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_
         return PYSPEC_E_WORKSPACE;
     }
     PYSPEC_CUDA(cudaMemcpyAsync(d_pair, hp->pair_ij.data(), hp->pair_ij.size() * 2, cudaMemcpyHostToDevice, st));
-    PYSPEC_CUDA(cudaMemcpyAsync(d_tri, hp->tri_of.data(), hp->tri_of.size() * 4, cudaMemcpyHostToDevice, st));
+    PYSPEC_CUDA(cudaMemcpyAsync(d_slot, hp->slot_of.data(), hp->slot_of.size() * 4, cudaMemcpyHostToDevice, st));
+    PYSPEC_CUDA(cudaMemcpyAsync(d_stri, hp->slot_tri.data(), hp->slot_tri.size() * 4, cudaMemcpyHostToDevice, st));
     PYSPEC_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), st));
     PYSPEC_CUDA(cudaMemsetAsync(partials, 0, (size_t)gx * ntri * sizeof(double), st));
     Params P = hp->base;
@@ -682,7 +701,8 @@ int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_
     P.nchunks = nchunks;
     P.chunks_per_cta = (nchunks + gx - 1) / gx;
     P.pair_ij = d_pair;
-    P.tri_of = d_tri;
+    P.slot_of = d_slot;
+    P.slot_tri = d_stri;
     P.partials = partials;
     P.err = d_err;
     PYSPEC_TRY(allow_smem((const void*)contract_tc_kernel, hp->smem));
