@@ -35,6 +35,11 @@ WORKLOAD = {"workload": "zeldovich-1M-360-step3-nmax40", "npart": 1_000_000, "Lb
             "step": 3, "Ncut": 3, "Nmax": 40, "triangles": 6350, "shells": 40,
             "field": "GRF P(k)~k^-1.5 on 360^3, rms displacement 5 Mpc/h, lattice 100^3 with random offsets",
             "seed": 2}
+# a reduced case of the same kernels for ncu captures (fields 283 MB, still > L2);
+# its line is not a bench result
+SMALL_WORKLOAD = {"workload": "zeldovich-300k-192-step3-nmax40 (profiling case)", "npart": 300_000,
+                  "Lbox": 1500.0, "Ngrid": 192, "step": 3, "Ncut": 3, "Nmax": 40, "triangles": 6350, "shells": 40,
+                  "field": "GRF P(k)~k^-1.5 on 192^3, rms displacement 5 Mpc/h", "seed": 2}
 L2_FLUSH_BYTES = 512 << 20   # > 129 MB L2, written between timed steps
 
 
@@ -292,7 +297,7 @@ def run_gpu(args, rank, world, local_rank):
     # work = 2 T V useful FLOP (one FMA per triangle and voxel); executed tensor
     # work = 2 x 3 products x (sum of tile M x N) x V.
     V = n ** 3
-    useful = 2.0 * 6350 * V
+    useful = 2.0 * plans["bf16x3"].T * V
     tiles_mn = 128 * (16 + 32 + 32 + 48)
     executed = 2.0 * 3 * tiles_mn * V
     t_con = main["stage_ms"]["contraction"] / 1e3
@@ -333,7 +338,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--small", action="store_true", help="run the 192^3 profiling case instead of the bench workload")
     args = ap.parse_args()
+    if args.small:
+        WORKLOAD.clear()
+        WORKLOAD.update(SMALL_WORKLOAD)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

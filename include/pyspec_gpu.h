@@ -144,6 +144,8 @@ int pyspec_shell_fields(const float *half, int ngrid, int step, int jmin, int nm
  *   fields 16-byte aligned, N^3 divisible by 4; returns PYSPEC_E_UNSUPPORTED
  *   otherwise).  After the stream has run a BF16X3 call, the int32 at
  *   workspace offset 0 is 0, or the code of a bounded wait that timed out.
+ * The triangles of one list must be distinct (as unordered shell triples):
+ *   a repeated triangle returns PYSPEC_E_INVALID with either planned method.
  * ---------------------------------------------------------------------- */
 size_t pyspec_bk_contract_workspace(int ngrid, int nshell, int ntri, int method);
 int pyspec_bk_contract(const float *fields, int ngrid, int nshell, const int32_t *tri,
@@ -223,6 +225,19 @@ int pyspec_pk_monopole(const float *half, int ngrid, double lbox, double *out, v
  * ---------------------------------------------------------------------- */
 int pyspec_pk_pbox_rsd(const float *half, int ngrid, int irsd, int lbox, int nbin, int nmu,
                        double *out, void *stream);
+
+/* ------------------------------------------------------------------------
+ * P(k, mu) with the reference's numpy binning -- pyspectrum.py:545-611
+ * (_Pk_periodic_rsd with code='python'), on a FULL grid delta(k) complex64
+ * (N, N, N) [z][y][x]: Nbins = N/2 bins irk = int(Nbins*|k|/k_Nyq + 0.5),
+ * mu from the folded components in float64, mu bins ceil(mu/dmu).
+ * lbox <= 0 means no box size (kf = 1).  out: 2*tot doubles,
+ * tot = 5*(N/2) + 4*(N/2)*nmu, results first, in the order
+ * k, p0, p2, p4, nk [N/2]; k_kmu, mu_kmu, p_kmu, n_kmu [N/2][nmu],
+ * with the (2 pi)^3 factor applied (no shot noise subtracted).
+ * ---------------------------------------------------------------------- */
+int pyspec_pk_rsd_python(const float *full, int ngrid, int irsd, double lbox, int nmu,
+                         double *out, void *stream);
 
 #ifdef __cplusplus
 }

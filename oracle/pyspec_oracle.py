@@ -471,6 +471,62 @@ def pk_pbox_rsd(delt, irsd, Lbox, Nbin, Nmu, Ngrid):
     return k, p0, p2, p4, nk, km, mk, pkm, nkm
 
 
+def pk_rsd_python(delta, Lbox=None, rsd=2, Nmubin=5):
+    """pyspectrum.py:545-611 (_Pk_periodic_rsd with code='python') on a full
+    grid delta [x, y, z]: |k| bins irk = int(Nbins |k| / k_Nyq + 0.5) and
+    mu from the folded components |k_x|, |k_y|, |k_z| in float64 (so mu >= 0),
+    mu bins imu = ceil(mu / dmu); modes with imu = 0 count in Nk but add to
+    neither the (k, mu) table nor P2, P4 (the reference sums those inside its
+    mu-bin loop).  |delta| is the float32 modulus squared in float32, as
+    np.absolute on complex64.  Returns the 9 arrays after the (2 pi)^3 factor."""
+    n = delta.shape[0]
+    nb = n // 2
+    dmu = 1.0 / float(Nmubin)
+    kf = 1.0 if Lbox is None else 2 * np.pi / float(Lbox)
+    nyq = kf * float(n) / 2.0
+    a = np.minimum(np.arange(n), n - np.arange(n))
+    d2 = a[:, None, None] ** 2 + a[None, :, None] ** 2 + a[None, None, :] ** 2
+    rk = kf * np.sqrt(d2.astype(np.float64))
+    irk = (nb * rk / nyq + 0.5).astype(np.int64)
+    th = [0.5 * np.pi, 0.5 * np.pi, 0.0][rsd]
+    ph = [0.0, 0.5 * np.pi, 0.0][rsd]
+    rkx = kf * a[:, None, None]
+    rky = kf * a[None, :, None]
+    rkz = kf * a[None, None, :]
+    with np.errstate(invalid="ignore", divide="ignore"):
+        cos_t = rkz / rk
+        sin_t = np.sqrt(1.0 - cos_t ** 2)
+        cos_p = rkx / (rk * sin_t)
+        sin_p = rky / (rk * sin_t)
+        cc = np.where(sin_t > 0, np.sin(ph) * sin_p + np.cos(ph) * cos_p, 0.0)
+        mu = np.cos(th) * cos_t + np.sin(th) * sin_t * cc
+        imu = np.where(d2 == 0, -999, np.ceil(mu / dmu)).astype(np.int64)
+    leg2 = -0.5 + 1.5 * mu ** 2
+    leg4 = 0.375 - 3.75 * mu ** 2 + 4.375 * mu ** 4
+    p = (np.absolute(delta.astype(np.complex64)) ** 2).astype(np.float32).astype(np.float64)
+    sel = (irk >= 1) & (irk <= nb)
+    I = irk[sel] - 1
+    bs = lambda w: np.bincount(I, weights=w, minlength=nb)[:nb]
+    nk = bs(np.ones(I.shape))
+    ks = bs(rk[sel]); p0 = bs(p[sel])
+    selm = sel & (imu >= 1) & (imu <= Nmubin)
+    J = (irk[selm] - 1) * Nmubin + imu[selm] - 1
+    bm = lambda w: np.bincount(J, weights=w, minlength=nb * Nmubin)[: nb * Nmubin].reshape(nb, Nmubin)
+    nkm = bm(np.ones(J.shape)); km = bm(rk[selm]); mm = bm(mu[selm]); pkm = bm(p[selm])
+    Ik = irk[selm] - 1
+    p2 = np.bincount(Ik, weights=p[selm] * leg2[selm], minlength=nb)[:nb]
+    p4 = np.bincount(Ik, weights=p[selm] * leg4[selm], minlength=nb)[:nb]
+    kf3 = kf ** 3
+    norm = (2.0 * np.pi) ** 3
+    m = nk > 0
+    ks[m] /= nk[m]; p0[m] = p0[m] / nk[m] / kf3
+    p2[m] = p2[m] / nk[m] / kf3 * 5.0; p4[m] = p4[m] / nk[m] / kf3 * 9.0
+    p2[~m] = 0; p4[~m] = 0
+    q = nkm > 0
+    km[q] /= nkm[q]; mm[q] /= nkm[q]; pkm[q] = pkm[q] / nkm[q] / kf3
+    return ks, p0 * norm, p2 * norm, p4 * norm, nk, km, mm, pkm * norm, nkm
+
+
 def Pk_periodic_rsd(xyz, w=None, Lbox=2600, Ngrid=360, rsd=2, Nmubin=10, delta_half=None):
     """pyspectrum.py:460-538 with code='fortran' (pyspectrum.py:628-641)."""
     npart = np.asarray(xyz).shape[1] if xyz is not None else 0

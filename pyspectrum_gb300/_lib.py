@@ -43,6 +43,7 @@ SIGNATURES = {
     "pyspec_bk_normalize": (c_int, [_P, _P, _P, _P, _P, c_int, c_int, c_int, c_int, c_int, c_double, c_double, _P, _P]),
     "pyspec_pk_monopole": (c_int, [_P, c_int, c_double, _P, _P]),
     "pyspec_pk_pbox_rsd": (c_int, [_P, c_int, c_int, c_int, c_int, c_int, _P, _P]),
+    "pyspec_pk_rsd_python": (c_int, [_P, c_int, c_int, c_double, c_int, _P, _P]),
 }
 
 CONTRACT_FP32 = 0

@@ -138,19 +138,34 @@ def triangle_counts(Ngrid: int, Nmax: int, Ncut: int, step: int, device=None, us
     if use_disk and os.path.exists(path):
         z = np.load(path)
         res = (z["counts"].astype(np.int64), z["nk"].astype(np.int64))
-    else:
-        res = compute_triangle_counts(*key, device=device)
-        if use_disk:
-            try:
-                os.makedirs(cache_dir(), exist_ok=True)
-                tmp = path + ".tmp.npz"
-                np.savez(tmp, counts=res[0], nk=res[1])
-                os.replace(tmp, path)
-            except OSError:
-                pass
-    with _counts_lock:
-        _counts_mem[key] = res
+        with _counts_lock:
+            _counts_mem[key] = res
+        return res
+    res = compute_triangle_counts(*key, device=device)
+    install_triangle_counts(*key, res[0], res[1], use_disk=use_disk)
     return res
+
+
+def install_triangle_counts(Ngrid, Nmax, Ncut, step, counts, nk, use_disk: bool = True) -> None:
+    """Make (counts[T] in loop order, nk[Nmax+1]) the cached counts of a
+    geometry, in memory and (``use_disk``) in ``cache_dir()``."""
+    key = (int(Ngrid), int(Nmax), int(Ncut), int(step))
+    counts = np.asarray(counts, dtype=np.int64)
+    nk = np.asarray(nk, dtype=np.int64)
+    T = triangles(Ncut // step, Nmax).shape[1]
+    if counts.shape != (T,) or nk.shape != (Nmax + 1,):
+        raise ValueError(f"counts must have shape ({T},) and nk ({Nmax + 1},)")
+    if use_disk:
+        path = counts_path(*key)
+        try:
+            os.makedirs(cache_dir(), exist_ok=True)
+            tmp = path + ".tmp.npz"
+            np.savez(tmp, counts=counts, nk=nk)
+            os.replace(tmp, path)
+        except OSError:
+            pass
+    with _counts_lock:
+        _counts_mem[key] = (counts, nk)
 
 
 def compute_triangle_counts(Ngrid, Nmax, Ncut, step, device=None):
@@ -271,6 +286,23 @@ def pk_monopole(half: torch.Tensor, Lbox: float) -> np.ndarray:
     out = torch.empty((6, n // 2), dtype=torch.float64, device=half.device)
     call("pyspec_pk_monopole", ptr(half), n, float(Lbox), ptr(out), stream_ptr())
     return out[:3].cpu().numpy()
+
+
+def pk_rsd_python(full: torch.Tensor, irsd: int, Lbox, Nmu: int):
+    """The code='python' (k, mu) binning of pyspectrum.py:545-611 on a full
+    grid complex64 (N, N, N) [z, y, x]; the 9 arrays with (2 pi)^3 applied."""
+    n = full.shape[0]
+    nbin = n // 2
+    tot = 5 * nbin + 4 * nbin * Nmu
+    out = torch.empty(2 * tot, dtype=torch.float64, device=full.device)
+    call("pyspec_pk_rsd_python", ptr(full), n, int(irsd), -1.0 if Lbox is None else float(Lbox), int(Nmu), ptr(out),
+         stream_ptr())
+    o = out[:tot].cpu().numpy()
+    k, p0, p2, p4, nk = (o[i * nbin:(i + 1) * nbin] for i in range(5))
+    M = nbin * Nmu
+    base = 5 * nbin
+    km, mk, pkm, nkm = (o[base + i * M: base + (i + 1) * M].reshape(nbin, Nmu) for i in range(4))
+    return k, p0, p2, p4, nk, km, mk, pkm, nkm
 
 
 def pk_pbox_rsd(half: torch.Tensor, irsd: int, Lbox, Nmu: int):

@@ -14,6 +14,11 @@ void set_error(const char* fmt, ...);
 void count_launch(int n = 1);
 // Raises the dynamic shared-memory limit of a kernel once per process.
 int allow_smem(const void* func, size_t bytes);
+// Page-locked copy of a host byte range that lives as long as the process
+// (plans that own one are cached for the process lifetime), so the per-call
+// table upload is one asynchronous DMA copy.  Returns NULL if the host
+// allocation fails; callers then copy from their pageable buffer.
+void* pinned_copy(const void* src, size_t bytes);
 
 #define PYSPEC_CHECK_ARG(cond, ...)                          \
     do {                                                     \

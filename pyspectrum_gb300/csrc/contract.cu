@@ -9,6 +9,7 @@
 // folded into a Kahan-compensated float32 running sum; each CTA writes one
 // float64 partial per triangle and a second kernel adds the CTA partials in a
 // fixed order (float64, deterministic).
+#include <string.h>
 #include <algorithm>
 #include <map>
 #include <mutex>
@@ -259,9 +260,14 @@ __global__ void __launch_bounds__(MAXT, 1) contract_fp32_kernel(const __grid_con
     }
 }
 
+static size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
+
 struct HostPlan {
     std::vector<int16_t> rows, l0;
     std::vector<int32_t> tri;
+    std::vector<char> image;          // rows | l0 | tri, each 256-byte aligned (device layout)
+    const void* image_src = nullptr;  // page-locked copy of `image` (or image.data())
+    size_t off_l0 = 0, off_tri = 0;
     int ntile = 0;
     bool ok = false;
 };
@@ -277,11 +283,20 @@ static HostPlan* plan(int nshell, const int32_t* tri_host, int ntri) {
     if (it != g_plans.end()) return it->second;
     HostPlan* hp = new HostPlan();
     std::map<std::pair<int, int>, std::vector<std::pair<int, int>>> pairs;
+    std::map<std::pair<int, int>, std::vector<bool>> seen;
     bool ok = true;
     for (int t = 0; t < ntri; ++t) {
         int v[3] = {tri_host[t], tri_host[ntri + t], tri_host[2 * ntri + t]};
-        if (v[0] < 0 || v[1] < 0 || v[2] < 0 || v[0] >= nshell || v[1] >= nshell || v[2] >= nshell) continue;
+        if (v[0] < 0 || v[1] < 0 || v[2] < 0 || v[0] >= nshell || v[1] >= nshell || v[2] >= nshell)
+            continue;     // documented: such a triangle gets bsum = 0
         std::sort(v, v + 3);
+        std::vector<bool>& sv = seen[{v[2], v[1]}];
+        if (sv.empty()) sv.assign(nshell, false);
+        if (sv[v[0]]) {
+            ok = false;   // the same triangle twice
+            continue;
+        }
+        sv[v[0]] = true;
         pairs[{v[2], v[1]}].push_back({v[0], t});
     }
     std::vector<std::pair<int, int>> order;
@@ -311,12 +326,18 @@ static HostPlan* plan(int nshell, const int32_t* tri_host, int ntri) {
             ++hp->ntile;
         }
     }
+    hp->off_l0 = al(hp->rows.size() * 2);
+    hp->off_tri = hp->off_l0 + al(hp->l0.size() * 2);
+    hp->image.assign(hp->off_tri + al(hp->tri.size() * 4), 0);
+    memcpy(hp->image.data(), hp->rows.data(), hp->rows.size() * 2);
+    memcpy(hp->image.data() + hp->off_l0, hp->l0.data(), hp->l0.size() * 2);
+    memcpy(hp->image.data() + hp->off_tri, hp->tri.data(), hp->tri.size() * 4);
+    hp->image_src = pinned_copy(hp->image.data(), hp->image.size());
+    if (hp->image_src == nullptr) hp->image_src = hp->image.data();
     hp->ok = ok;
     g_plans[key] = hp;
     return hp;
 }
-
-static size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
 
 static void grid_dims(int64_t nvox, int ntile, int* gx, int* gy, int* per) {
     *gy = std::max(1, (ntile + MAXT - 1) / MAXT);
@@ -346,22 +367,25 @@ int contract_fp32_impl(const float* fields, int64_t nvox, int nshell, const int3
     PYSPEC_CHECK_ARG(tri_host != nullptr, "the FP32 contraction needs the host copy of the triangle list");
     PYSPEC_CHECK_ARG(nvox % 4 == 0 && ((uintptr_t)fields & 15) == 0, "fields must be 16-byte aligned, N^3 % 4 == 0");
     HostPlan* hp = plan(nshell, tri_host, ntri);
+    if (!hp->ok) {
+        set_error("the triangle list repeats a triangle");
+        return PYSPEC_E_INVALID;
+    }
     int gx, gy, per;
     grid_dims(nvox, hp->ntile, &gx, &gy, &per);
     char* w = reinterpret_cast<char*>(ws);
     size_t off = 0;
-    int16_t* d_rows = reinterpret_cast<int16_t*>(w + off); off += al(hp->rows.size() * 2);
-    int16_t* d_l0 = reinterpret_cast<int16_t*>(w + off); off += al(hp->l0.size() * 2);
-    int32_t* d_tri = reinterpret_cast<int32_t*>(w + off); off += al(hp->tri.size() * 4);
+    int16_t* d_rows = reinterpret_cast<int16_t*>(w + off);
+    int16_t* d_l0 = reinterpret_cast<int16_t*>(w + off + hp->off_l0);
+    int32_t* d_tri = reinterpret_cast<int32_t*>(w + off + hp->off_tri);
+    off += hp->image.size();
     double* partials = reinterpret_cast<double*>(w + off);
     off += al((size_t)gx * ntri * sizeof(double));
     if (off > ws_bytes) {
         set_error("contract workspace %zu bytes < required %zu", ws_bytes, off);
         return PYSPEC_E_WORKSPACE;
     }
-    PYSPEC_CUDA(cudaMemcpyAsync(d_rows, hp->rows.data(), hp->rows.size() * 2, cudaMemcpyHostToDevice, st));
-    PYSPEC_CUDA(cudaMemcpyAsync(d_l0, hp->l0.data(), hp->l0.size() * 2, cudaMemcpyHostToDevice, st));
-    PYSPEC_CUDA(cudaMemcpyAsync(d_tri, hp->tri.data(), hp->tri.size() * 4, cudaMemcpyHostToDevice, st));
+    PYSPEC_CUDA(cudaMemcpyAsync(d_rows, hp->image_src, hp->image.size(), cudaMemcpyHostToDevice, st));
     PYSPEC_CUDA(cudaMemsetAsync(partials, 0, (size_t)gx * ntri * sizeof(double), st));
     Params P;
     P.fields = fields;

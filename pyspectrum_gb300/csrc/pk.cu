@@ -162,6 +162,105 @@ __global__ void pk_rsd_finalize(const double* __restrict__ acc, int nbin, int nm
     }
 }
 
+// pyspectrum.py:545-611 (_Pk_periodic_rsd, code='python'): the numpy binning
+// over a FULL grid, in float64 with the reference's operation order (no fused
+// multiply-add): irk = int(Nbins*rk/k_Nyq + 0.5), mu from the folded (non-
+// negative) components, imu = ceil(mu/dmu).  Modes with imu outside
+// [1, Nmu] count in Nk but add to neither the (k, mu) table nor P2/P4.
+struct RsdPyConst {
+    double kf, nyq, dmu;
+    double ct, st, cph, sph;   // cos/sin of the observer's theta and phi (float64)
+};
+
+__global__ void pk_rsd_python_kernel(const float2* __restrict__ full, int n, int nbin, int nmu, RsdPyConst c,
+                                     double* __restrict__ acc) {
+    extern __shared__ double sm[];
+    double* b_nk = sm;
+    double* b_k = b_nk + nbin;
+    double* b_p0 = b_k + nbin;
+    double* b_p2 = b_p0 + nbin;
+    double* b_p4 = b_p2 + nbin;
+    double* m_n = b_p4 + nbin;
+    double* m_k = m_n + nbin * nmu;
+    double* m_mu = m_k + nbin * nmu;
+    double* m_p = m_mu + nbin * nmu;
+    const int tot = 5 * nbin + 4 * nbin * nmu;
+    for (int i = threadIdx.x; i < tot; i += blockDim.x) sm[i] = 0;
+    __syncthreads();
+    const int z = blockIdx.x;
+    const int az = foldi(z, n);
+    const double rkz = __dmul_rn(c.kf, (double)az);
+    for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+        const int y = i / n, x = i - y * n;
+        const int ax = foldi(x, n), ay = foldi(y, n);
+        const int64_t d2 = (int64_t)ax * ax + (int64_t)ay * ay + (int64_t)az * az;
+        const double rk = __dmul_rn(c.kf, __dsqrt_rn((double)d2));
+        const int irk = (int)__dadd_rn(__ddiv_rn(__dmul_rn((double)nbin, rk), c.nyq), 0.5);
+        if (irk < 1 || irk > nbin) continue;
+        const double cos_t = __ddiv_rn(rkz, rk);
+        const double sin_t = __dsqrt_rn(__dsub_rn(1.0, __dmul_rn(cos_t, cos_t)));
+        double cc = 0.0;
+        if (sin_t > 0.0) {
+            const double den = __dmul_rn(rk, sin_t);
+            const double cp = __ddiv_rn(__dmul_rn(c.kf, (double)ax), den);
+            const double sp = __ddiv_rn(__dmul_rn(c.kf, (double)ay), den);
+            cc = __dadd_rn(__dmul_rn(c.sph, sp), __dmul_rn(c.cph, cp));
+        }
+        const double mu = __dadd_rn(__dmul_rn(c.ct, cos_t), __dmul_rn(__dmul_rn(c.st, sin_t), cc));
+        const int imu = (int)ceil(__ddiv_rn(mu, c.dmu));
+        const float2 v = full[((int64_t)z * n + y) * n + x];
+        const float am = hypotf(v.x, v.y);
+        const double p = (double)(am * am);
+        const int b = irk - 1;
+        atomicAdd(&b_nk[b], 1.0);
+        atomicAdd(&b_k[b], rk);
+        atomicAdd(&b_p0[b], p);
+        if (imu >= 1 && imu <= nmu) {
+            const double mu2 = __dmul_rn(mu, mu);
+            const double le2 = __dadd_rn(-0.5, __dmul_rn(1.5, mu2));
+            const double le4 = __dadd_rn(__dsub_rn(0.375, __dmul_rn(3.75, mu2)), __dmul_rn(4.375, __dmul_rn(mu2, mu2)));
+            atomicAdd(&b_p2[b], __dmul_rn(p, le2));
+            atomicAdd(&b_p4[b], __dmul_rn(p, le4));
+            const int m = b * nmu + imu - 1;
+            atomicAdd(&m_n[m], 1.0);
+            atomicAdd(&m_k[m], rk);
+            atomicAdd(&m_mu[m], mu);
+            atomicAdd(&m_p[m], p);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < tot; i += blockDim.x)
+        if (sm[i] != 0.0) atomicAdd(&acc[i], sm[i]);
+}
+
+// averages and the (2 pi)^3 / kf^3 factors of pyspectrum.py:588-609
+__global__ void pk_rsd_python_finalize(const double* __restrict__ acc, int nbin, int nmu, double kf3,
+                                       double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const double tp = 2.0 * 3.14159265358979323846;
+    const double norm = tp * tp * tp;
+    if (i < nbin) {
+        const double c = acc[i];
+        const bool ok = c > 0;
+        out[i] = ok ? acc[nbin + i] / c : 0.0;
+        out[nbin + i] = ok ? acc[2 * nbin + i] / c / kf3 * norm : 0.0;
+        out[2 * nbin + i] = ok ? acc[3 * nbin + i] / c / kf3 * 5.0 * norm : 0.0;
+        out[3 * nbin + i] = ok ? acc[4 * nbin + i] / c / kf3 * 9.0 * norm : 0.0;
+        out[4 * nbin + i] = c;
+    }
+    if (i < nbin * nmu) {
+        const double* a = acc + 5 * nbin;
+        double* o = out + 5 * nbin;
+        const int M = nbin * nmu;
+        const double c = a[i];
+        const bool ok = c > 0;
+        o[i] = ok ? a[M + i] / c : 0.0;
+        o[M + i] = ok ? a[2 * M + i] / c : 0.0;
+        o[2 * M + i] = ok ? a[3 * M + i] / c / kf3 * norm : 0.0;
+        o[3 * M + i] = c;
+    }
+}
+
 }  // namespace pyspec
 
 using namespace pyspec;
@@ -221,6 +320,41 @@ extern "C" int pyspec_pk_pbox_rsd(const float* half, int ngrid, int irsd, int lb
     PYSPEC_LAUNCH_CHECK();
     const int m = nbin * nmu > nbin ? nbin * nmu : nbin;
     pk_rsd_finalize<<<(m + 127) / 128, 128, 0, st>>>(acc, nbin, nmu, c.kf, out);
+    PYSPEC_LAUNCH_CHECK();
+    count_launch(2);
+    return PYSPEC_OK;
+}
+
+extern "C" int pyspec_pk_rsd_python(const float* full, int ngrid, int irsd, double lbox, int nmu, double* out,
+                                    void* stream) {
+    PYSPEC_CHECK_ARG(full && out, "NULL pointer");
+    PYSPEC_CHECK_ARG(ngrid >= 4 && ngrid % 2 == 0, "ngrid=%d must be even", ngrid);
+    PYSPEC_CHECK_ARG(irsd >= 0 && irsd <= 2, "irsd must be 0, 1 or 2");
+    PYSPEC_CHECK_ARG(nmu >= 1, "bad nmu");
+    const int nbin = ngrid / 2;
+    const size_t tot = 5 * (size_t)nbin + 4 * (size_t)nbin * nmu;
+    const size_t sm = sizeof(double) * tot;
+    PYSPEC_CHECK_ARG(sm <= 200 * 1024, "nbin*nmu too large for one CTA's histogram");
+    cudaStream_t st = as_stream(stream);
+    double* acc = out + tot;
+    PYSPEC_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * tot, st));
+    // pyspectrum.py:551-567: kf = 1 without a box size
+    const double pi = 3.14159265358979323846;
+    RsdPyConst c;
+    c.kf = lbox > 0 ? 2.0 * pi / lbox : 1.0;
+    c.nyq = c.kf * (double)ngrid / 2.0;
+    c.dmu = 1.0 / (double)nmu;
+    const double theta = irsd == 2 ? 0.0 : 0.5 * pi;
+    const double phi = irsd == 1 ? 0.5 * pi : 0.0;
+    c.ct = cos(theta);
+    c.st = sin(theta);
+    c.cph = cos(phi);
+    c.sph = sin(phi);
+    PYSPEC_TRY(allow_smem((const void*)pk_rsd_python_kernel, sm));
+    pk_rsd_python_kernel<<<ngrid, 256, sm, st>>>(reinterpret_cast<const float2*>(full), ngrid, nbin, nmu, c, acc);
+    PYSPEC_LAUNCH_CHECK();
+    const int m = nbin * nmu > nbin ? nbin * nmu : nbin;
+    pk_rsd_python_finalize<<<(m + 127) / 128, 128, 0, st>>>(acc, nbin, nmu, c.kf * c.kf * c.kf, out);
     PYSPEC_LAUNCH_CHECK();
     count_launch(2);
     return PYSPEC_OK;

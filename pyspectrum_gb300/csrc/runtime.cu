@@ -63,4 +63,14 @@ int allow_smem(const void* func, size_t bytes) {
     PYSPEC_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     return PYSPEC_OK;
 }
+
+void* pinned_copy(const void* src, size_t bytes) {
+    void* p = nullptr;
+    if (bytes == 0 || cudaHostAlloc(&p, bytes, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();   // clear a failed allocation's sticky-free error state
+        return nullptr;
+    }
+    memcpy(p, src, bytes);
+    return p;
+}
 }  // namespace pyspec

@@ -9,23 +9,31 @@ CUDA behind a C ABI).  Differences from the reference, all deliberate:
   aligned (the reference appends zeros to its value arrays but not to its
   index arrays for zero-count triangles, pyspectrum.py:438-445).
 * ``Pk_periodic`` bins the reflected grid (the reference indexes the half
-  grid with a full-grid mask at pyspectrum.py:713, which raises).
+  grid with a full-grid mask at pyspectrum.py:713, which raises); so does
+  ``Pk_periodic_rsd(code='python')`` (its numpy binning, pyspectrum.py:545-611,
+  cannot index the half grid it is handed).
 * ``fft`` and ``nthreads`` are accepted and ignored: every FFT is the
   library's own.  ``method`` selects the contraction ('fp32' CUDA cores or
   'bf16x3' tensor cores).
 * ``Bk_periodic_rsd`` is new (the reference composes applyRSD + Bk_periodic).
+* ``Bk_periodic_batch`` is new: many boxes of mixed grid sizes per call
+  (CUDA-graph replay of the per-geometry stages).
 * ``Ncut // step`` must be >= 1.
 """
 from __future__ import annotations
+
+import os
 
 import numpy as np
 import torch
 
 from . import core
+from .batch import Bk_periodic_batch  # noqa: F401  (many boxes per call; no reference counterpart)
 from .util import applyRSD  # noqa: F401  (re-exported as the tests of the reference expect)
 
 __all__ = ["FFT_periodic", "FFTperiodic", "reflect_delta", "Pk_periodic", "Pk_periodic_rsd", "_Pk_periodic_rsd",
-           "Bk_periodic", "_Bk_periodic", "Bk_periodic_rsd", "_counts_Bk123", "applyRSD"]
+           "Bk_periodic", "_Bk_periodic", "Bk_periodic_rsd", "_counts_Bk123", "_counts_Bk123_f77",
+           "applyRSD", "Bk_periodic_batch"]
 
 
 def _np_weights(w, n):
@@ -73,16 +81,37 @@ def reflect_delta(delt, Ngrid=360, silent=True, device=None):
     return np.ascontiguousarray(full.cpu().numpy().transpose(2, 1, 0))
 
 
-def _counts_Bk123(Ngrid=360, Nmax=40, Ncut=3, step=3, fft='pyfftw', silent=True, device=None):
+def _counts_Bk123(Ngrid=360, Nmax=40, Ncut=3, step=3, fft='pyfftw', silent=True, device=None, dat_dir=None):
     """pyspectrum.py:962-1030: (Nmax, Nmax, Nmax) float64 array with
     counts[i-1, j-1, l-1] = sum_x I_i I_j I_l = N^3 x (number of closed
-    k-triangles), for the triangle loop's (i, j, l)."""
-    jmin = Ncut // step
-    c, _ = core.triangle_counts(Ngrid, Nmax, Ncut, step, device=device)
-    tri = core.triangles(jmin, Nmax)
-    out = np.zeros((Nmax, Nmax, Nmax))
-    out[tri[0] - 1, tri[1] - 1, tri[2] - 1] = c.astype(np.float64) * float(Ngrid) ** 3
+    k-triangles), for the triangle loop's (i, j, l).
+
+    With ``dat_dir`` the reference's cache convention applies: an existing
+    ``counts.Ngrid..{fft}`` file there is read and returned as stored (and its
+    rounded counts become this package's cache for the geometry); otherwise
+    the counts are computed and written there in the reference's format."""
+    from . import counts_cache as cc
+    if dat_dir is not None:
+        path = os.path.join(dat_dir, cc.reference_counts_name(Ngrid, Nmax, Ncut, step, fft))
+        if os.path.isfile(path):
+            arr = cc.read_reference_counts(path, Nmax, fft)
+            counts = cc.counts_from_reference_array(arr, Ngrid, Nmax, Ncut, step)
+            core.install_triangle_counts(Ngrid, Nmax, Ncut, step, counts, cc.mode_counts_host(Ngrid, step, Nmax))
+            return arr
+        if not silent:
+            print("--- calculating %s ---" % path)
+    out = cc.reference_counts_array(Ngrid, Nmax, Ncut, step, device=device)
+    if dat_dir is not None:
+        cc.write_reference_counts(path, out, fft)
     return out
+
+
+def _counts_Bk123_f77(Ngrid=360, Nmax=40, Ncut=3, step=3, silent=True, device=None, dat_dir=None):
+    """pyspectrum.py:1033-1056 (Fortran bk_counts, estimator.f:2-102): the same
+    normalisation in the layout the reference's fort77 cache reader returns
+    (values at [i-1, j-1, l-1] for i >= j >= l).  With ``dat_dir`` the
+    ``counts...fort77`` file there is read, or written after computing."""
+    return _counts_Bk123(Ngrid, Nmax, Ncut, step, fft='fort77', silent=silent, device=device, dat_dir=dat_dir)
 
 
 def _bk_from_half(half, Ngrid, step, Ncut, Nmax, method, units=None, device=None):
@@ -128,10 +157,24 @@ def Bk_periodic(xyz, w=None, Lbox=2600, Ngrid=360, step=3, Ncut=3, Nmax=40, fft=
 
 
 def _Pk_periodic_rsd(delta, Lbox=None, rsd=2, Nmubin=5, code='fortran', device=None):
-    """pyspectrum.py:541-641 (code='fortran' path, estimator.f:155-264) on the
-    half grid delta (N//2+1, N, N) [x, y, z]; includes the (2 pi)^3 factor."""
+    """pyspectrum.py:541-641, both binnings; includes the (2 pi)^3 factor.
+
+    code='fortran' (estimator.f:155-264): ``delta`` is the half grid
+    (N//2+1, N, N) [x, y, z].  code='python' (pyspectrum.py:545-611): ``delta``
+    is a full grid (N, N, N) [x, y, z], binned with the reference's numpy rules
+    (float64 mu from folded components, ceil(mu/dmu) bins, no shot noise).
+    A CUDA tensor is taken as already on the device in [z, y, x] order."""
+    if code == 'python':
+        if torch.is_tensor(delta):
+            full = delta
+        else:
+            a = np.asarray(delta, dtype=np.complex64)
+            if a.ndim != 3 or not (a.shape[0] == a.shape[1] == a.shape[2]):
+                raise ValueError("code='python' bins a full (N, N, N) grid")
+            full = torch.as_tensor(a).permute(2, 1, 0).contiguous().to(core._dev(device))
+        return core.pk_rsd_python(full, rsd, Lbox, Nmubin)
     if code != 'fortran':
-        raise NotImplementedError("only the code='fortran' binning (estimator.f:155-264) is provided")
+        raise ValueError("code must be 'fortran' or 'python'")
     half = _half_from_numpy(delta, device) if not torch.is_tensor(delta) else delta
     k, p0k, p2k, p4k, nk, k_kmu, mu_kmu, p_kmu, n_kmu = core.pk_pbox_rsd(half, rsd, Lbox, Nmubin)
     norm = (2. * np.pi) ** 3
@@ -141,7 +184,11 @@ def _Pk_periodic_rsd(delta, Lbox=None, rsd=2, Nmubin=5, code='fortran', device=N
 def _pk_rsd_dict(half, N, Lbox, Ngrid, rsd, Nmubin, code):
     nbar = float(N) / Lbox ** 3        # pyspectrum.py:510 (particle count, not sum w)
     kf = 2 * np.pi / Lbox
-    k, p0k, p2k, p4k, n_k, k_kmu, mu_kmu, p_kmu, n_kmu = _Pk_periodic_rsd(half, Lbox=Lbox, rsd=rsd, Nmubin=Nmubin,
+    # code='python' bins the full grid (the reference hands it FFT_periodic's
+    # half grid, which its numpy binning cannot index; the reflected grid is
+    # what that code is written for)
+    grid = core.reflect_half(half) if code == 'python' else half
+    k, p0k, p2k, p4k, n_k, k_kmu, mu_kmu, p_kmu, n_kmu = _Pk_periodic_rsd(grid, Lbox=Lbox, rsd=rsd, Nmubin=Nmubin,
                                                                           code=code)
     return {'meta': {'Lbox': Lbox, 'Ngrid': Ngrid, 'N': N, 'nbar': nbar, 'kf': kf},
             'k': k, 'p0k': p0k - 1. / nbar, 'p2k': p2k, 'p4k': p4k, 'p_sn': np.repeat(1. / nbar, len(k)),

@@ -2,7 +2,7 @@
 
 Run once in a checkout that has the reference source tree (read-only is fine):
 
-    PYSPEC_REFERENCE=<path to pySpectrum checkout> python tests/golden/make_golden.py
+    PYSPEC_REFERENCE=<path to pySpectrum checkout> python tests/golden/make_golden.py [pk_rsd_python]
 
 What it produces (all small, committed):
 
@@ -18,6 +18,9 @@ What it produces (all small, committed):
 * ``ref_fft_small.npz`` -- the reference's ``_FFT`` (de-interleave +
   unnormalised backward FFT) on a seeded interlaced grid.
 * ``ref_rsd.npz`` -- the reference's ``util.applyRSD`` on fixture halos.
+* ``ref_pk_rsd_python.npz`` -- the reference's ``_Pk_periodic_rsd`` with
+  ``code='python'`` (its numpy (k, mu) binning) on seeded full delta(k)
+  grids at N = 16, 24 for every line of sight.
 * ``test_box_f32.npz`` -- the reference's test fixture ``dat/test_box.hdf5``
   (73,442 halo positions and velocities, L = 2600), read from its raw HDF5
   data offsets and stored as float32.
@@ -180,11 +183,33 @@ def fixture_and_rsd(ref_util, FlatLambdaCDM):
     np.savez_compressed(os.path.join(HERE, "ref_rsd.npz"), **out)
 
 
+def pk_rsd_python_goldens(ref):
+    import contextlib
+    import io
+    out = {}
+    cases = [(16, 4, 0), (16, 5, 1), (24, 4, 2), (24, 3, 0)]
+    out["cases"] = np.array(cases)
+    for n, nmu, rsd in cases:
+        rng = np.random.default_rng(500 + n + nmu + rsd)
+        full = (np.fft.fftn(rng.standard_normal((n, n, n)) + 0.2) / n ** 1.5).astype(np.complex64)
+        with contextlib.redirect_stdout(io.StringIO()):      # the reference prints every bin
+            res = ref._Pk_periodic_rsd(full, Lbox=1000.0, rsd=rsd, Nmubin=nmu, code="python")
+        tag = f"n{n}_m{nmu}_r{rsd}"
+        out[tag + "_delta"] = full
+        for name, v in zip(("k", "p0k", "p2k", "p4k", "nk", "k_kmu", "mu_kmu", "p_kmu", "n_kmu"), res):
+            out[tag + "_" + name] = np.asarray(v)
+    np.savez_compressed(os.path.join(HERE, "ref_pk_rsd_python.npz"), **out)
+
+
 def main():
     FlatLambdaCDM = _install_stubs()
     sys.path.insert(0, REF)
     from pyspectrum import pyspectrum as ref
     from pyspectrum import util as ref_util
+    if sys.argv[1:] == ["pk_rsd_python"]:           # only this fixture
+        pk_rsd_python_goldens(ref)
+        return
+    pk_rsd_python_goldens(ref)
     counts_goldens()
     with tempfile.TemporaryDirectory() as tmp:
         bk_goldens(ref, tmp)

@@ -79,3 +79,40 @@ def test_bf16x3_rejects_unsupported():
     rc = lib.pyspec_bk_contract(ptr(fields), n, 70, ptr(tri_d), slots.ctypes.data_as(ctypes.c_void_p), T, 1,
                                 ptr(bsum), ptr(ws), ws.numel(), stream_ptr())
     assert rc == -3
+
+
+def test_arbitrary_triangle_lists():
+    """A shuffled subset of the loop's triangles, with the shells of each
+    triangle in any order and gaps in each pair's column range: both planned
+    methods against float64."""
+    n, step, nmax, jmin = 48, 1, 24, 1
+    fields = _fields(n, step, jmin, nmax, seed=7)
+    tri = core.triangles(jmin, nmax) - jmin
+    rng = np.random.default_rng(3)
+    keep = rng.permutation(tri.shape[1])[: tri.shape[1] // 3]
+    sub = tri[:, keep]
+    for t in range(sub.shape[1]):
+        sub[:, t] = sub[rng.permutation(3), t]
+    slots = np.ascontiguousarray(sub, dtype=np.int32)
+    ref, mag = _reference(fields, slots)
+    mag = np.maximum(mag, 1e-300)
+    for method, tol in ((0, 1e-6), (1, 3e-5)):
+        got, status = _contract(fields, n, slots, method)
+        assert status == 0
+        assert (np.abs(got - ref) / mag).max() < tol, method
+
+
+@pytest.mark.parametrize("method", [0, 1])
+def test_repeated_triangle_rejected(method):
+    n = 16
+    fields = torch.zeros((8, n ** 3), dtype=torch.float32, device="cuda")
+    slots = np.ascontiguousarray(core.triangles(1, 8) - 1, dtype=np.int32)
+    slots = np.ascontiguousarray(np.concatenate([slots, slots[:, 5:6][[2, 0, 1]]], axis=1))
+    lib = load()
+    T = slots.shape[1]
+    tri_d = torch.from_numpy(slots).cuda()
+    bsum = torch.zeros(T, dtype=torch.float64, device="cuda")
+    ws = torch.zeros(lib.pyspec_bk_contract_workspace(n, 8, T, method), dtype=torch.uint8, device="cuda")
+    rc = lib.pyspec_bk_contract(ptr(fields), n, 8, ptr(tri_d), slots.ctypes.data_as(ctypes.c_void_p), T, method,
+                                ptr(bsum), ptr(ws), ws.numel(), stream_ptr())
+    assert rc == -1

@@ -1,0 +1,90 @@
+"""The 512^3 / step 2 / Nmax 60 geometry (60 shells, 20,275 triangles; 32 GB of
+float32 shell fields) on a 16,003,008-particle Zel'dovich box (L = 3000).
+
+Checks that hold at this size:
+* triangle counts: exact against a direct enumeration of closed k-triangles
+  (k1 + k2 + k3 = 0 with |k_a| in shells i, j, l; the definition behind
+  pyspectrum.py:976-1023) for the low triangles, and integral everywhere;
+* mode counts Nk against the host count;
+* the two contraction forms against each other on every triangle, and both
+  against float64 sums (complex128 shell FFTs of the same delta(k)) on the
+  triangles of shells 1-3."""
+import numpy as np
+import pytest
+import scipy.fft as sfft
+
+from oracle import pyspec_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+N, L, STEP, NCUT, NMAX = 512, 3000.0, 2, 3, 60
+
+
+def _shell_modes(j, step, n):
+    """Integer wave vectors (components in [-n/2, n/2)) of shell j."""
+    r = int(np.ceil((j + 0.5) * step)) + 1
+    a = np.arange(-r, r + 1)
+    k = np.stack(np.meshgrid(a, a, a, indexing="ij"), -1).reshape(-1, 3)
+    d2 = (k ** 2).sum(1)
+    sh = O.shell_index_int(d2, step)
+    return k[sh == j]
+
+
+def _count_closed(i, j, l, step):
+    ki, kj, kl = (_shell_modes(s, step, N) for s in (i, j, l))
+    R = 4 * (i + 1) * step + 4          # bounds every component of k1 + k2
+    key = lambda v: ((v[..., 0] + R) * (2 * R + 1) + (v[..., 1] + R)) * (2 * R + 1) + (v[..., 2] + R)
+    k3 = -(ki[:, None, :] + kj[None, :, :]).reshape(-1, 3)
+    return int(np.isin(key(k3), key(kl)).sum())
+
+
+def test_512_nmax60_counts_contraction_and_fp64():
+    import torch
+    from pyspectrum_gb300 import core, counts_cache, mocks
+    jmin = NCUT // STEP
+    counts, nk = core.triangle_counts(N, NMAX, NCUT, STEP, use_disk=False)
+    loop = core.triangles(jmin, NMAX)
+    assert loop.shape[1] == 20275 and counts.shape == (20275,)
+    np.testing.assert_array_equal(nk, counts_cache.mode_counts_host(N, STEP, NMAX))
+    for t in range(loop.shape[1]):
+        i, j, l = (int(v) for v in loop[:, t])
+        if i <= 3:
+            assert counts[t] == _count_closed(i, j, l, STEP), (i, j, l)
+    assert (counts > 0).all()
+
+    x = mocks.zeldovich_mock(16_003_008, L, ngrid=N, seed=5)
+    xyzs, ws = core.prepare_positions(x, L)
+    half = core.fft_periodic_half(xyzs, ws, N, L, float(x.shape[1]))
+    del x, xyzs, ws
+    bs = {}
+    for method in ("fp32", "bf16x3"):
+        plan = core.get_plan(N, STEP, NCUT, NMAX, method)
+        plan.run(half)
+        torch.cuda.synchronize()
+        bs[method] = plan.bsum.cpu().numpy()
+        assert np.isfinite(bs[method]).all()
+    core.release_plans()
+    torch.cuda.empty_cache()
+    rel = np.abs(bs["bf16x3"] - bs["fp32"]) / np.abs(bs["fp32"])
+    assert np.median(rel) < 1e-4, np.median(rel)
+
+    # float64 reference sums for the triangles of shells 1-3
+    full = O.reflect_delta(half.cpu().numpy().transpose(2, 1, 0), N)
+    del half
+    kk = np.minimum(np.arange(N), N - np.arange(N)).astype(np.int64)
+    d2 = kk[:, None, None] ** 2 + kk[None, :, None] ** 2 + kk[None, None, :] ** 2
+    irk = O.shell_index_int(d2, STEP)
+    del d2
+    F = {}
+    for j in (1, 2, 3):
+        F[j] = np.real(sfft.fftn(np.where(irk == j, full, 0).astype(np.complex128), workers=-1)).ravel()
+    del full, irk
+    for t in range(loop.shape[1]):
+        i, j, l = (int(v) for v in loop[:, t])
+        if i > 3:
+            continue
+        prod = F[i] * F[j] * F[l]
+        exact, absum = prod.sum(), np.abs(prod).sum()
+        for method in ("fp32", "bf16x3"):
+            err = abs(bs[method][t] - exact) / absum
+            assert err < (2e-6 if method == "fp32" else 2e-5), (method, i, j, l, err)
