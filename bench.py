@@ -295,19 +295,20 @@ def run_gpu(args, rank, world, local_rank):
     main = results["bf16x3"]
     # roofline of the dominant kernel: the tensor-core contraction.  Algorithmic
     # work = 2 T V useful FLOP (one FMA per triangle and voxel); executed tensor
-    # work = 2 x 3 products x (sum of tile M x N) x V.
+    # work = 2 FLOP x 2 A parts (hi, lo) x (sum over tiles of M x 2N: hi and lo
+    # B columns) x V, with 128-row tiles of N = 16, 32, 32, 48 shells.
     V = n ** 3
     useful = 2.0 * plans["bf16x3"].T * V
-    tiles_mn = 128 * (16 + 32 + 32 + 48)
-    executed = 2.0 * 3 * tiles_mn * V
+    tiles_mn = 128 * 2 * (16 + 32 + 32 + 48)
+    executed = 2.0 * 2 * tiles_mn * V
     t_con = main["stage_ms"]["contraction"] / 1e3
     roofline = {"kernel": "contract_tc_kernel (+ partial reduction)", "bound": "tensor",
                 "achieved": useful / t_con / 1e12, "peak": bf16, "unit": "TFLOP/s",
                 "frac": useful / t_con / 1e12 / bf16, "peak_kind": kind,
                 "executed_tflops": executed / t_con / 1e12, "executed_frac": executed / t_con / 1e12 / bf16,
                 "useful_over_executed": useful / executed,
-                "traffic": 4.0 * 40 * V, "traffic_note": "dram bytes of one launch, scaled from the ncu "
-                "capture at 192^3 by the voxel count (fields are read once)"}
+                "traffic": 4.0 * 40 * V, "traffic_note": "dram bytes of one launch: the ncu capture at 192^3 "
+                "(1.133 GB read) scaled by the voxel count; equal to the algorithmic bytes (fields read once)"}
     cpu = None
     if not args.no_cpu_baseline:
         total, det, sample, cores = cpu_reference_sample(xyz_np)
@@ -331,6 +332,35 @@ def run_gpu(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+def run_profile_shells(jtop):
+    """Profiling case for the shell passes: shells jtop-2..jtop of the bench
+    workload's delta(k) at 360^3 (about 1 GB on the device), three calls.
+    Prints the time of the last call; not a bench result."""
+    import torch
+    from pyspectrum_gb300 import _lib, core
+    from pyspectrum_gb300._lib import call, ptr, stream_ptr
+    W = WORKLOAD
+    n, L, step = W["Ngrid"], W["Lbox"], W["step"]
+    x, _ = make_positions_np(W["seed"])
+    xyzs, ws = core.prepare_positions(x, L)
+    half = core.fft_periodic_half(xyzs, ws, n, L, float(x.shape[1]))
+    del x, xyzs, ws
+    jmin, nmax = jtop - 2, jtop
+    S = nmax - jmin + 1
+    fields = torch.empty((S, n ** 3), dtype=torch.float32, device=half.device)
+    p0 = torch.empty(S, dtype=torch.float64, device=half.device)
+    wsb = torch.empty(_lib.load().pyspec_shell_fields_workspace(n, S), dtype=torch.uint8, device=half.device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(3):
+        e0.record()
+        call("pyspec_shell_fields", ptr(half), n, step, jmin, nmax, ptr(fields), ptr(p0), ptr(wsb), wsb.numel(),
+             stream_ptr())
+        e1.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "shell_fields", "Ngrid": n, "shells": [jmin, nmax],
+                      "ms_last_call": e0.elapsed_time(e1)}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -339,7 +369,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="run the 192^3 profiling case instead of the bench workload")
+    ap.add_argument("--profile-shells", type=int, default=0, metavar="J",
+                    help="only run shells J-2..J of the bench workload three times (ncu profiling case)")
     args = ap.parse_args()
+    if args.profile_shells:
+        run_profile_shells(args.profile_shells)
+        return
     if args.small:
         WORKLOAD.clear()
         WORKLOAD.update(SMALL_WORKLOAD)

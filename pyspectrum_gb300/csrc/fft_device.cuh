@@ -6,6 +6,8 @@
 // DFT and writes them Ns apart into the other buffer (self-sorting, so no bit
 // reversal).  Twiddles come from a per-CTA table tw[m] = exp(sign*2*pi*i*m/n).
 #pragma once
+#include <type_traits>
+#include <utility>
 #include "common.cuh"
 
 namespace pyspec {
@@ -103,6 +105,105 @@ __device__ __forceinline__ void dft8(C* v, int sign) {
         v[k] = cadd(e[k], o[k]);
         v[k + 4] = csub(e[k], o[k]);
     }
+}
+
+// ---------------------------------------------------------------------------
+// Composite radices R = A*B evaluated in registers (one Cooley-Tukey step):
+//   X[k1 + A k2] = DFT_B over n2 of ( W_R^(n2 k1) * DFT_A over n1 of x[B n1 + n2] )
+// so a Stockham stage of radix 12, 15, 16, ... replaces two stages of the
+// small radices (one pass over shared memory instead of two).  The inner
+// twiddles W_R^m are compile-time constants from a constexpr Taylor series
+// (double precision, rounded once to T).
+// ---------------------------------------------------------------------------
+namespace twc {
+constexpr double kPi = 3.14159265358979323846;
+// sin / cos of x in [-pi, pi] by their Taylor series (terms up to x^41)
+constexpr double sin_(double x) {
+    double term = x, sum = x;
+    for (int k = 1; k <= 20; ++k) { term *= -x * x / ((2.0 * k) * (2.0 * k + 1.0)); sum += term; }
+    return sum;
+}
+constexpr double cos_(double x) {
+    double term = 1.0, sum = 1.0;
+    for (int k = 1; k <= 20; ++k) { term *= -x * x / ((2.0 * k - 1.0) * (2.0 * k)); sum += term; }
+    return sum;
+}
+// angle 2 pi m / R reduced to (-pi, pi]
+constexpr double angle(int m, int R) {
+    int mm = m % R;
+    if (2 * mm > R) mm -= R;
+    return 2.0 * kPi * (double)mm / (double)R;
+}
+}  // namespace twc
+
+// W_R^M = exp(2 pi i M / R) as compile-time constants
+template <typename T, int R, int M>
+struct Tw {
+    static constexpr T c = (T)twc::cos_(twc::angle(M, R));
+    static constexpr T s = (T)twc::sin_(twc::angle(M, R));
+};
+
+// compile-time loop: f(std::integral_constant<int, I>) for I = 0..N-1
+template <typename F, int... I>
+__device__ __forceinline__ void static_for_(F&& f, std::integer_sequence<int, I...>) {
+    (f(std::integral_constant<int, I>{}), ...);
+}
+template <int N, typename F>
+__device__ __forceinline__ void static_for(F&& f) {
+    static_for_(f, std::make_integer_sequence<int, N>{});
+}
+
+template <typename T, typename C, int R>
+__device__ __forceinline__ void small_dft(C* v, int sign);
+
+template <typename T, typename C, int A, int B>
+__device__ __forceinline__ void dft_composite(C* v, int sign) {
+    constexpr int R = A * B;
+    C y[R];
+    static_for<B>([&](auto n2c) {
+        constexpr int n2 = decltype(n2c)::value;
+        C t[A];
+#pragma unroll
+        for (int n1 = 0; n1 < A; ++n1) t[n1] = v[B * n1 + n2];
+        small_dft<T, C, A>(t, sign);
+        static_for<A>([&](auto k1c) {
+            constexpr int k1 = decltype(k1c)::value;
+            constexpr int m = (n2 * k1) % R;
+            if constexpr (m == 0) {
+                y[n2 * A + k1] = t[k1];
+            } else {
+                const C w = mk<T>(Tw<T, R, m>::c, sign > 0 ? Tw<T, R, m>::s : -Tw<T, R, m>::s);
+                y[n2 * A + k1] = cmul(t[k1], w);
+            }
+        });
+    });
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) {
+        C u[B];
+#pragma unroll
+        for (int n2 = 0; n2 < B; ++n2) u[n2] = y[n2 * A + k1];
+        small_dft<T, C, B>(u, sign);
+#pragma unroll
+        for (int k2 = 0; k2 < B; ++k2) v[k1 + A * k2] = u[k2];
+    }
+}
+
+template <typename T, typename C, int R>
+__device__ __forceinline__ void small_dft(C* v, int sign) {
+    if constexpr (R == 2) dft2<T>(v);
+    else if constexpr (R == 3) dft3<T>(v, sign);
+    else if constexpr (R == 4) dft4<T>(v, sign);
+    else if constexpr (R == 5) dft5<T>(v, sign);
+    else if constexpr (R == 8) dft8<T>(v, sign);
+    else if constexpr (R == 6) dft_composite<T, C, 3, 2>(v, sign);
+    else if constexpr (R == 9) dft_composite<T, C, 3, 3>(v, sign);
+    else if constexpr (R == 10) dft_composite<T, C, 5, 2>(v, sign);
+    else if constexpr (R == 12) dft_composite<T, C, 4, 3>(v, sign);
+    else if constexpr (R == 15) dft_composite<T, C, 5, 3>(v, sign);
+    else if constexpr (R == 16) dft_composite<T, C, 4, 4>(v, sign);
+    else if constexpr (R == 20) dft_composite<T, C, 5, 4>(v, sign);
+    else if constexpr (R == 24) dft_composite<T, C, 8, 3>(v, sign);
+    else static_assert(R == 2, "unsupported radix");
 }
 
 // Twiddle table tw[m] = exp(sign * 2*pi*i * m / n), m in [0, n).
@@ -203,13 +304,29 @@ namespace ct {
 
 constexpr int kRadices[5] = {8, 4, 5, 3, 2};
 
+// Stage radices for the common lengths (composite radices: fewer passes over
+// shared memory); other lengths factor greedily into 8, 4, 5, 3, 2.
+struct Plan { int n, len, r[4]; };
+constexpr Plan kPlans[] = {
+    {360, 3, {12, 5, 6, 0}}, {180, 2, {12, 15, 0, 0}},
+    {192, 2, {16, 12, 0, 0}}, {96, 2, {8, 12, 0, 0}},
+    {256, 2, {16, 16, 0, 0}}, {128, 2, {16, 8, 0, 0}},
+};
+constexpr int find_plan(int n) {
+    for (int i = 0; i < (int)(sizeof(kPlans) / sizeof(kPlans[0])); ++i)
+        if (kPlans[i].n == n) return i;
+    return -1;
+}
+
 constexpr int nstages(int n) {
+    if (find_plan(n) >= 0) return kPlans[find_plan(n)].len;
     int m = n, s = 0;
     for (int k = 0; k < 5; ++k)
         while (m % kRadices[k] == 0) { m /= kRadices[k]; ++s; }
     return m == 1 ? s : -1;
 }
 constexpr int radix_at(int n, int stage) {
+    if (find_plan(n) >= 0) return kPlans[find_plan(n)].r[stage];
     int m = n, s = 0;
     for (int k = 0; k < 5; ++k)
         while (m % kRadices[k] == 0) {
@@ -256,11 +373,7 @@ __device__ __forceinline__ typename cplx_t<T>::type* stages(typename cplx_t<T>::
 #pragma unroll
                 for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * k * twstep]);
             }
-            if constexpr (R == 2) dft2<T>(v);
-            else if constexpr (R == 3) dft3<T>(v, sign);
-            else if constexpr (R == 4) dft4<T>(v, sign);
-            else if constexpr (R == 5) dft5<T>(v, sign);
-            else dft8<T>(v, sign);
+            small_dft<T, C, R>(v, sign);
             C* d = dst + line * ls;
             const int base = jb * Ns * R + k;
 #pragma unroll

@@ -36,6 +36,14 @@ __host__ __device__ inline int64_t shell_d2hi(int j, int step) {
 
 __device__ __forceinline__ int fold(int i, int n) { return i <= n - i ? i : n - i; }
 
+// Row stride (in complex elements) of the work grid: n/2+1 rounded up so that
+// every row starts on a 16-byte boundary (the x pass copies rows in 16-byte
+// pieces).
+template <typename C>
+__host__ __device__ constexpr int work_stride(int n) {
+    return sizeof(C) == 8 ? (n / 2 + 1) + ((n / 2 + 1) & 1) : n / 2 + 1;
+}
+
 // rows of the x pass handled by one CTA
 __host__ __device__ constexpr int xpass_rows_ct(int n) {
     return (4096 / n) < 1 ? 1 : ((4096 / n) > 16 ? 16 : 4096 / n);
@@ -77,6 +85,9 @@ __global__ void __launch_bounds__(256) shell_zpass_kernel(const typename cplx_t<
     const int ncol = min(tx, nh - x0);
     const int64_t zstride = (int64_t)n * nh;
     const int64_t base = (int64_t)y * nh + x0;
+    const int ws = work_stride<C>(n);
+    const int64_t wzstride = (int64_t)n * ws;
+    const int64_t wbase = (int64_t)y * ws + x0;
     for (int i = threadIdx.x; i < n * tx; i += blockDim.x) {
         const int z = i / tx, c = i - z * tx;
         C v = mk<T>(0, 0);
@@ -94,9 +105,18 @@ __global__ void __launch_bounds__(256) shell_zpass_kernel(const typename cplx_t<
     C* res;
     if constexpr (NC > 0) res = ct::fft_tile_ct<T, NC, tx, 0>(buf0, buf1, tw, -1);
     else res = fft_tile<T, tx>(buf0, buf1, tw, plan, tx, -1);
-    for (int i = threadIdx.x; i < n * tx; i += blockDim.x) {
-        const int z = i / tx, c = i - z * tx;
-        if (c < ncol) work[base + z * zstride + c] = res[i];
+    // pairs of elements per store where a pair is 16 bytes (rows of the work
+    // grid are 16-byte aligned and padded, x0 is even)
+    constexpr int VEC = sizeof(C) == 8 ? 2 : 1;
+    for (int i = threadIdx.x; i < n * (tx / VEC); i += blockDim.x) {
+        const int z = i / (tx / VEC), c = (i - z * (tx / VEC)) * VEC;
+        if (c >= ncol) continue;
+        if constexpr (VEC == 2) {
+            const C a = res[z * tx + c], b = res[z * tx + c + 1];
+            *reinterpret_cast<float4*>(&work[wbase + z * wzstride + c]) = make_float4(a.x, a.y, b.x, b.y);
+        } else {
+            work[wbase + z * wzstride + c] = res[z * tx + c];
+        }
     }
 }
 
@@ -116,32 +136,37 @@ __global__ void __launch_bounds__(256) shell_ypass_kernel(typename cplx_t<T>::ty
     C* buf1 = buf0 + (size_t)tx * n;
     copy_table(tw, twg, n);
     const int ncol = min(tx, nh - x0);
-    const int64_t base = (int64_t)z * n * nh + x0;
-    for (int i = threadIdx.x; i < n * tx; i += blockDim.x) {
-        const int y = i / tx, c = i - y * tx;
+    const int ws = work_stride<C>(n);
+    const int64_t base = (int64_t)z * n * ws + x0;
+    constexpr int VEC = sizeof(C) == 8 ? 2 : 1;   // elements per 16-byte access
+    for (int i = threadIdx.x; i < n * (tx / VEC); i += blockDim.x) {
+        const int y = i / (tx / VEC), c = (i - y * (tx / VEC)) * VEC;
         const int yf = fold(y, n);
-        C v = mk<T>(0, 0);
         // rows the z pass did not visit hold zeros
-        if (c < ncol && (int64_t)x0 * x0 + (int64_t)yf * yf <= d2hi) v = work[base + (int64_t)y * nh + c];
-        buf0[i] = v;
+        const bool live = c < ncol && (int64_t)x0 * x0 + (int64_t)yf * yf <= d2hi;
+        if constexpr (VEC == 2) {
+            float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (live) q = *reinterpret_cast<const float4*>(&work[base + (int64_t)y * ws + c]);
+            buf0[y * tx + c] = mk<T>(q.x, q.y);
+            buf0[y * tx + c + 1] = mk<T>(q.z, q.w);
+        } else {
+            buf0[y * tx + c] = live ? work[base + (int64_t)y * ws + c] : mk<T>(0, 0);
+        }
     }
     __syncthreads();
     C* res;
     if constexpr (NC > 0) res = ct::fft_tile_ct<T, NC, tx, 0>(buf0, buf1, tw, -1);
     else res = fft_tile<T, tx>(buf0, buf1, tw, plan, tx, -1);
-    for (int i = threadIdx.x; i < n * tx; i += blockDim.x) {
-        const int y = i / tx, c = i - y * tx;
-        if (c < ncol) work[base + (int64_t)y * nh + c] = res[i];
+    for (int i = threadIdx.x; i < n * (tx / VEC); i += blockDim.x) {
+        const int y = i / (tx / VEC), c = (i - y * (tx / VEC)) * VEC;
+        if (c >= ncol) continue;
+        if constexpr (VEC == 2) {
+            const C a = res[y * tx + c], b = res[y * tx + c + 1];
+            *reinterpret_cast<float4*>(&work[base + (int64_t)y * ws + c]) = make_float4(a.x, a.y, b.x, b.y);
+        } else {
+            work[base + (int64_t)y * ws + c] = res[y * tx + c];
+        }
     }
-}
-
-// Asynchronous copy of one complex element (8 or 16 bytes); bytes = 0 zero-fills.
-template <typename C>
-__device__ __forceinline__ void cp_async_elem(uint32_t dst, const void* src, int bytes) {
-    if constexpr (sizeof(C) == 8)
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" :: "r"(dst), "l"(src), "r"(bytes) : "memory");
-    else
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" :: "r"(dst), "l"(src), "r"(bytes) : "memory");
 }
 
 // x rows: a persistent CTA walks blocks of RL consecutive rows r = z*n + y.
@@ -157,28 +182,33 @@ __global__ void __launch_bounds__(256) shell_xpass_kernel(const typename cplx_t<
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = NC > 0 ? NC : n_rt;
     const int rl = NC > 0 ? xpass_rows_ct(NC) : rl_rt;
-    const int nh = n / 2 + 1, h = n / 2;
+    const int h = n / 2;
+    const int ws = work_stride<C>(n);          // row stride of the work grid and the staging rows
     C* twN = reinterpret_cast<C*>(smem_raw);   // exp(-2 pi i m / n), m < n
     C* twH = twN + n;                          // exp(-2 pi i m / (n/2))
-    C* stage0 = twH + h;                       // 2 x rl * nh
-    C* buf0 = stage0 + 2 * (size_t)rl * nh;    // rl * h
+    // 2 x rl * ws staging rows, 16-byte aligned for the asynchronous copies
+    C* stage0 = reinterpret_cast<C*>((reinterpret_cast<uintptr_t>(twH + h) + 15) & ~(uintptr_t)15);
+    C* buf0 = stage0 + 2 * (size_t)rl * ws;    // rl * h
     C* buf1 = buf0 + (size_t)rl * h;
     __shared__ double red[32];
     copy_table(twN, twg, n + h);               // both tables are contiguous
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
     const int64_t nrows = (int64_t)n * n;
     const int64_t nblocks = (nrows + rl - 1) / rl;
+    // 16-byte pieces of a row holding its first xlim elements (the rest is
+    // treated as zero when the row is packed)
+    const int npiece = (int)(((size_t)xlim * sizeof(C) + 15) / 16);
     auto issue = [&](int64_t blk, int sbuf) {
         if (blk < nblocks) {
             const int64_t r0 = blk * rl;
             const int nr = (int)min((int64_t)rl, nrows - r0);
-            C* st = stage0 + (size_t)sbuf * rl * nh;
+            C* st = stage0 + (size_t)sbuf * rl * ws;
             for (int rr = warp; rr < nr; rr += nwarp) {
-                const C* src = work + (r0 + rr) * nh;
-                const uint32_t dst = (uint32_t)__cvta_generic_to_shared(st + rr * nh);
-                for (int x = lane; x < nh; x += 32)
-                    cp_async_elem<C>(dst + (uint32_t)(x * sizeof(C)), x < xlim ? (const void*)(src + x) : (const void*)src,
-                                     x < xlim ? (int)sizeof(C) : 0);
+                const char* src = reinterpret_cast<const char*>(work + (r0 + rr) * ws);
+                const uint32_t dst = (uint32_t)__cvta_generic_to_shared(st + rr * ws);
+                for (int q = lane; q < npiece; q += 32)
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" :: "r"(dst + (uint32_t)(q * 16)),
+                                 "l"(src + (size_t)q * 16) : "memory");
             }
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
@@ -192,12 +222,13 @@ __global__ void __launch_bounds__(256) shell_xpass_kernel(const typename cplx_t<
         __syncthreads();
         const int64_t r0 = blk * rl;
         const int nr = (int)min((int64_t)rl, nrows - r0);
-        const C* st = stage0 + (size_t)sb * rl * nh;
+        const C* st = stage0 + (size_t)sb * rl * ws;
         for (int rr = warp; rr < nr; rr += nwarp) {
-            const C* X = st + rr * nh;
+            const C* X = st + rr * ws;
             C* out = buf0 + rr * h;
             for (int k = lane; k < h; k += 32) {
-                C a = X[k], b = X[h - k];
+                C a = k < xlim ? X[k] : mk<T>(0, 0);
+                C b = h - k < xlim ? X[h - k] : mk<T>(0, 0);
                 if (k == 0) { a.y = 0; b.y = 0; }
                 const C bc = mk<T>(b.x, -b.y);
                 const C e = cadd(a, bc);
@@ -226,6 +257,85 @@ __global__ void __launch_bounds__(256) shell_xpass_kernel(const typename cplx_t<
         double v = threadIdx.x < nwarp ? red[threadIdx.x] : 0.0;
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (threadIdx.x == 0) part[blockIdx.x] = v;
+    }
+}
+
+// x rows for the common grid sizes, with the half-length FFT of H = R1*R2
+// points done in registers: a warp transforms two rows at a time (16 lanes
+// per row).  Stage 1 loads its inputs straight from the work grid, forms
+// Z[k] (the C2R packing above) and applies radix-R1 butterflies; the outputs
+// cross lanes once through a padded per-row buffer in shared memory (one pad
+// element per R1, so neither side has bank conflicts); stage 2 applies the
+// twiddles and radix-R2 butterflies and stores the row of F directly.  No
+// block-wide barrier: each warp only synchronises with itself.
+template <int NC, int R1, int R2>
+__global__ void __launch_bounds__(256) shell_xpass_reg_kernel(const float2* __restrict__ work, int xlim,
+                                                              float* __restrict__ field, double* __restrict__ part,
+                                                              const float2* __restrict__ twg) {
+    constexpr int N = NC, H = N / 2, WS = work_stride<float2>(N);
+    static_assert(R1 * R2 == H && R1 <= 16 && R2 <= 16, "two radix stages of at most 16 lanes");
+    constexpr int PADH = H + R2;                 // R2 butterflies x (R1 + 1) slots
+    __shared__ float2 twN[H];                    // exp(-2 pi i k / N), k < H
+    __shared__ float2 twH[H];                    // exp(-2 pi i m / H)
+    __shared__ float2 rowbuf[8][2][PADH];
+    __shared__ double red[8];
+    for (int i = threadIdx.x; i < H; i += blockDim.x) {
+        twN[i] = twg[i];
+        twH[i] = twg[N + i];
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = lane >> 4, t = lane & 15;
+    float2* buf = rowbuf[warp][sub];
+    const int64_t nrows = (int64_t)N * N;        // even: rows come in pairs
+    const int64_t nw = (int64_t)gridDim.x * 8;
+    float local = 0.f;
+    for (int64_t r0 = ((int64_t)blockIdx.x * 8 + warp) * 2; r0 < nrows; r0 += nw * 2) {
+        const int64_t row = r0 + sub;
+        const float2* X = work + row * WS;
+        if (t < R2) {
+            float2 v[R1];
+#pragma unroll
+            for (int r = 0; r < R1; ++r) {
+                const int k = t + r * R2;
+                float2 a = k < xlim ? X[k] : make_float2(0.f, 0.f);
+                float2 b = H - k < xlim ? X[H - k] : make_float2(0.f, 0.f);
+                if (k == 0) { a.y = 0.f; b.y = 0.f; }
+                const float2 bc = make_float2(b.x, -b.y);
+                const float2 e = cadd(a, bc);
+                const float2 o = cmul(csub(a, bc), twN[k]);
+                v[r] = make_float2(e.x - o.y, e.y + o.x);      // e + i*o
+            }
+            small_dft<float, float2, R1>(v, -1);
+#pragma unroll
+            for (int r = 0; r < R1; ++r) buf[t * (R1 + 1) + r] = v[r];   // element t*R1 + r
+        }
+        __syncwarp();
+        if (t < R1) {
+            float2 v[R2];
+#pragma unroll
+            for (int r = 0; r < R2; ++r) {
+                const float2 x = buf[t + r * (R1 + 1)];                   // element t + r*R1
+                v[r] = r == 0 ? x : cmul(x, twH[r * t]);                  // r*t < H
+            }
+            small_dft<float, float2, R2>(v, -1);
+            float2* out = reinterpret_cast<float2*>(field + row * N);
+#pragma unroll
+            for (int r = 0; r < R2; ++r) {
+                out[t + r * R1] = v[r];       // f[2m] = Re z[m], f[2m+1] = Im z[m]
+                local += v[r].x * v[r].x + v[r].y * v[r].y;
+            }
+        }
+        __syncwarp();                         // buf is rewritten for the next pair
+    }
+    double acc = (double)local;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) red[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double v = 0.0;
+        for (int w = 0; w < 8; ++w) v += red[w];
+        part[blockIdx.x] = v;
     }
 }
 
@@ -258,15 +368,18 @@ static int xpass_ctas(int n) {
 template <typename T>
 size_t shell_workspace_bytes(int n, int nshell) {
     using C = typename cplx_t<T>::type;
-    const size_t nh = n / 2 + 1;
     const size_t nblk = (size_t)xpass_ctas(n);
-    size_t b = nh * n * n * sizeof(C);
+    size_t b = (size_t)work_stride<C>(n) * n * n * sizeof(C);
     b = (b + 255) & ~(size_t)255;
     b += (size_t)nshell * nblk * sizeof(double);
     b = (b + 255) & ~(size_t)255;
     b += (size_t)(n + n / 2) * sizeof(C);          // twiddle tables
     return b;
 }
+
+// radix split H = R1 * R2 of the register x pass per grid size
+constexpr int XR1(int n) { return n == 360 ? 12 : n == 192 ? 8 : n == 256 ? 8 : n == 512 ? 16 : 1; }
+constexpr int XR2(int n) { return n == 360 ? 15 : n == 192 ? 12 : n == 256 ? 16 : n == 512 ? 16 : 1; }
 
 template <typename T, bool INDICATOR>
 int shell_one_impl(const typename cplx_t<T>::type* half, int n, int step, int j, T* field, double* part,
@@ -286,7 +399,7 @@ int shell_one_impl(const typename cplx_t<T>::type* half, int n, int step, int j,
     const size_t sm_zy = sizeof(C) * ((size_t)n + 2 * (size_t)tx * n);
     const int rl = xpass_rows(n);
     const int h = n / 2;
-    const size_t sm_x = sizeof(C) * ((size_t)n + h + 2 * (size_t)rl * nh + 2 * (size_t)rl * h);
+    const size_t sm_x = sizeof(C) * ((size_t)n + h + 2 * (size_t)rl * work_stride<C>(n) + 2 * (size_t)rl * h) + 16;
     const unsigned nblk = (unsigned)xpass_ctas(n);
     // compile-time plans for the common grid sizes (single precision)
 #define PYSPEC_SHELL_LAUNCH(NCV)                                                                          \
@@ -300,7 +413,12 @@ int shell_one_impl(const typename cplx_t<T>::type* half, int n, int step, int j,
         shell_ypass_kernel<T, NCV><<<(unsigned)(ntx_active * n), 256, sm_zy, st>>>(work, n, d2hi,         \
                                                                                    ntx_active, plan, tw); \
         PYSPEC_LAUNCH_CHECK();                                                                           \
-        shell_xpass_kernel<T, NCV><<<nblk, 256, sm_x, st>>>(work, n, xlim, rl, plan_half, field, part, tw); \
+        if constexpr (NCV > 0 && sizeof(T) == 4)                                                         \
+            shell_xpass_reg_kernel<NCV, XR1(NCV), XR2(NCV)><<<nblk, 256, 0, st>>>(                           \
+                reinterpret_cast<const float2*>(work), xlim, reinterpret_cast<float*>(field), part,          \
+                reinterpret_cast<const float2*>(tw));                                                    \
+        else                                                                                             \
+            shell_xpass_kernel<T, NCV><<<nblk, 256, sm_x, st>>>(work, n, xlim, rl, plan_half, field, part, tw); \
         PYSPEC_LAUNCH_CHECK();                                                                           \
     } while (0)
     bool done = false;
@@ -341,8 +459,7 @@ int shell_fields_impl(const typename cplx_t<T>::type* half, int n, int step, int
         return PYSPEC_E_WORKSPACE;
     }
     C* work = reinterpret_cast<C*>(ws);
-    const size_t nh = n / 2 + 1;
-    size_t off = (nh * n * n * sizeof(C) + 255) & ~(size_t)255;
+    size_t off = ((size_t)work_stride<C>(n) * n * n * sizeof(C) + 255) & ~(size_t)255;
     double* part = reinterpret_cast<double*>(reinterpret_cast<char*>(ws) + off);
     const int nblk = xpass_ctas(n);
     const int64_t V = (int64_t)n * n * n;

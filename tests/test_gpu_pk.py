@@ -71,10 +71,14 @@ def test_pk_rsd_python_binning_matches_reference(golden):
     for n, nmu, rsd in g["cases"]:
         tag = f"n{n}_m{nmu}_r{rsd}"
         got = P._Pk_periodic_rsd(g[tag + "_delta"], Lbox=1000.0, rsd=int(rsd), Nmubin=int(nmu), code="python")
+        scale = np.abs(g[tag + "_p0k"]).max()
         for name, v in zip(names, got):
             r = g[tag + "_" + name]
             if name in ("nk", "n_kmu"):
                 np.testing.assert_array_equal(v, r, err_msg=tag + name)
+            elif name in ("p2k", "p4k"):
+                # Legendre-weighted sums cancel: bound the error by the monopole scale
+                np.testing.assert_allclose(v, r, rtol=2e-6, atol=2e-6 * scale, err_msg=tag + name)
             else:
                 np.testing.assert_allclose(v, r, rtol=2e-6, atol=1e-9 * np.abs(r).max(), err_msg=tag + name)
 
