@@ -202,6 +202,7 @@ __device__ __forceinline__ void small_dft(C* v, int sign) {
     else if constexpr (R == 15) dft_composite<T, C, 5, 3>(v, sign);
     else if constexpr (R == 16) dft_composite<T, C, 4, 4>(v, sign);
     else if constexpr (R == 20) dft_composite<T, C, 5, 4>(v, sign);
+    else if constexpr (R == 18) dft_composite<T, C, 6, 3>(v, sign);
     else if constexpr (R == 24) dft_composite<T, C, 8, 3>(v, sign);
     else static_assert(R == 2, "unsupported radix");
 }

@@ -169,6 +169,87 @@ __global__ void __launch_bounds__(256) shell_ypass_kernel(typename cplx_t<T>::ty
     }
 }
 
+// z and y lines for the common grid sizes, in registers: a CTA transforms
+// the 8 columns x0..x0+7 of one tile (8 lines of length N = R1*R2) in two
+// radix stages.  Stage 1 loads its inputs straight from HBM (8 consecutive
+// columns = 64 contiguous bytes per row), applies radix-R1 butterflies and
+// writes them to a padded per-column buffer in shared memory; after one
+// barrier stage 2 applies the twiddles and radix-R2 butterflies and stores
+// the results straight to the work grid.  Thread t handles column t % 8.
+//   ZPASS: lines along z, input = delta(k) masked by the shell (or the shell
+//          indicator), output = work.  Tiles outside the shell return at once.
+//   else:  lines along y, in place in work; rows the z pass did not visit
+//          read as zeros.
+template <int NC, int R1, int R2>
+struct LinePassShape {
+    static constexpr int NB1 = NC / (R1 > 0 ? R1 : 1), NB2 = NC / (R2 > 0 ? R2 : 1);   // butterflies per line
+    static constexpr int THREADS = 8 * (NB1 > NB2 ? NB1 : NB2);
+    // padded column: element p at p + p / R1; stride == 2 (mod 16) complex so
+    // the 8 columns of a half-warp fall in different banks
+    static constexpr int COLP = ((NC + NB1 + 13) / 16) * 16 + 2;
+};
+
+template <int NC, int R1, int R2, bool ZPASS, bool INDICATOR>
+__global__ void __launch_bounds__(LinePassShape<NC, R1, R2>::THREADS)
+shell_line_pass_kernel(const float2* __restrict__ half, float2* __restrict__ work, int64_t d2lo, int64_t d2hi,
+                       int ntx_tiles, const float2* __restrict__ twg) {
+    using S = LinePassShape<NC, R1, R2>;
+    constexpr int N = NC, NH = N / 2 + 1, WS = work_stride<float2>(N);
+    static_assert(R1 * R2 == N, "two radix stages");
+    __shared__ float2 buf[8 * S::COLP];
+    const int tile = blockIdx.x % ntx_tiles;
+    const int other = blockIdx.x / ntx_tiles;   // y (z pass) or z (y pass)
+    const int x0 = tile * 8;
+    const int c = threadIdx.x & 7, b = threadIdx.x >> 3;
+    const int x = x0 + c;
+    const bool colok = x < NH;
+    const int of = fold(other, N);
+    if (ZPASS && (int64_t)x0 * x0 + (int64_t)of * of > d2hi) return;   // whole tile outside the shell
+    float2* col = buf + c * S::COLP;
+    // ---- stage 1: radix R1, butterfly b over elements b + r*NB1 ----
+    if (b < S::NB1) {
+        float2 v[R1];
+#pragma unroll
+        for (int r = 0; r < R1; ++r) {
+            const int e = b + r * S::NB1;       // position along the line
+            const int ef = fold(e, N);
+            float2 val = make_float2(0.f, 0.f);
+            if constexpr (ZPASS) {
+                const int64_t d2 = (int64_t)x * x + (int64_t)of * of + (int64_t)ef * ef;
+                if (colok && d2 >= d2lo && d2 <= d2hi) {
+                    if constexpr (INDICATOR) val = make_float2(1.f, 0.f);
+                    else val = half[((int64_t)e * N + other) * NH + x];
+                }
+            } else {
+                if (colok && (int64_t)x0 * x0 + (int64_t)ef * ef <= d2hi)
+                    val = work[((int64_t)other * N + e) * WS + x];
+            }
+            v[r] = val;
+        }
+        small_dft<float, float2, R1>(v, -1);
+#pragma unroll
+        for (int r = 0; r < R1; ++r) col[b * (R1 + 1) + r] = v[r];   // element b*R1 + r
+    }
+    __syncthreads();
+    // ---- stage 2: radix R2, butterfly j over elements j + r*NB2, twiddle exp(-2 pi i r j / N) ----
+    if (b < S::NB2 && colok) {
+        float2 v[R2];
+#pragma unroll
+        for (int r = 0; r < R2; ++r) {
+            const int p = b + r * S::NB2;                     // element index (< N)
+            const float2 u = col[p + p / R1];
+            v[r] = r == 0 || b == 0 ? u : cmul(u, __ldg(&twg[r * b]));
+        }
+        small_dft<float, float2, R2>(v, -1);
+#pragma unroll
+        for (int r = 0; r < R2; ++r) {
+            const int e = b + r * S::NB2;                       // output position along the line
+            if constexpr (ZPASS) work[((int64_t)e * N + other) * WS + x] = v[r];
+            else work[((int64_t)other * N + e) * WS + x] = v[r];
+        }
+    }
+}
+
 // x rows: a persistent CTA walks blocks of RL consecutive rows r = z*n + y.
 // The rows of the next block are copied into the other staging buffer with
 // cp.async while the current block is transformed, so the loads are always in
@@ -269,7 +350,7 @@ __global__ void __launch_bounds__(256) shell_xpass_kernel(const typename cplx_t<
 // twiddles and radix-R2 butterflies and stores the row of F directly.  No
 // block-wide barrier: each warp only synchronises with itself.
 template <int NC, int R1, int R2>
-__global__ void __launch_bounds__(256) shell_xpass_reg_kernel(const float2* __restrict__ work, int xlim,
+__global__ void __launch_bounds__(256, 4) shell_xpass_reg_kernel(const float2* __restrict__ work, int xlim,
                                                               float* __restrict__ field, double* __restrict__ part,
                                                               const float2* __restrict__ twg) {
     constexpr int N = NC, H = N / 2, WS = work_stride<float2>(N);
@@ -362,7 +443,7 @@ static int xpass_ctas(int n) {
     int sms = 152, dev = 0;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int64_t blocks = ((int64_t)n * n + xpass_rows(n) - 1) / xpass_rows(n);
-    return (int)std::min<int64_t>(blocks, (int64_t)sms * 3);
+    return (int)std::min<int64_t>(blocks, (int64_t)sms * 4);
 }
 
 template <typename T>
@@ -378,6 +459,9 @@ size_t shell_workspace_bytes(int n, int nshell) {
 }
 
 // radix split H = R1 * R2 of the register x pass per grid size
+// radix split N = R1 * R2 of the register z / y line pass per grid size (0: none)
+constexpr int LR1(int n) { return n == 360 ? 20 : n == 192 ? 16 : n == 256 ? 16 : 0; }
+constexpr int LR2(int n) { return n == 360 ? 18 : n == 192 ? 12 : n == 256 ? 16 : 1; }
 constexpr int XR1(int n) { return n == 360 ? 12 : n == 192 ? 8 : n == 256 ? 8 : n == 512 ? 16 : 1; }
 constexpr int XR2(int n) { return n == 360 ? 15 : n == 192 ? 12 : n == 256 ? 16 : n == 512 ? 16 : 1; }
 
@@ -407,12 +491,25 @@ int shell_one_impl(const typename cplx_t<T>::type* half, int n, int step, int j,
         PYSPEC_TRY(allow_smem((const void*)shell_zpass_kernel<T, INDICATOR, NCV>, sm_zy));               \
         PYSPEC_TRY(allow_smem((const void*)shell_ypass_kernel<T, NCV>, sm_zy));                          \
         PYSPEC_TRY(allow_smem((const void*)shell_xpass_kernel<T, NCV>, sm_x));                           \
-        shell_zpass_kernel<T, INDICATOR, NCV><<<(unsigned)(ntx * n), 256, sm_zy, st>>>(half, work, n, d2lo, \
-                                                                                         d2hi, plan, tw);   \
-        PYSPEC_LAUNCH_CHECK();                                                                           \
-        shell_ypass_kernel<T, NCV><<<(unsigned)(ntx_active * n), 256, sm_zy, st>>>(work, n, d2hi,         \
-                                                                                   ntx_active, plan, tw); \
-        PYSPEC_LAUNCH_CHECK();                                                                           \
+        if constexpr (LR1(NCV) > 0 && sizeof(T) == 4) {                                                   \
+            using LS = LinePassShape<NCV, LR1(NCV), LR2(NCV)>;                                            \
+            shell_line_pass_kernel<NCV, LR1(NCV), LR2(NCV), true, INDICATOR>                               \
+                <<<(unsigned)(ntx * n), LS::THREADS, 0, st>>>(reinterpret_cast<const float2*>(half),      \
+                    reinterpret_cast<float2*>(work), d2lo, d2hi, ntx, reinterpret_cast<const float2*>(tw)); \
+            PYSPEC_LAUNCH_CHECK();                                                                       \
+            shell_line_pass_kernel<NCV, LR1(NCV), LR2(NCV), false, INDICATOR>                              \
+                <<<(unsigned)(ntx_active * n), LS::THREADS, 0, st>>>(reinterpret_cast<const float2*>(half), \
+                    reinterpret_cast<float2*>(work), d2lo, d2hi, ntx_active,                             \
+                    reinterpret_cast<const float2*>(tw));                                                \
+            PYSPEC_LAUNCH_CHECK();                                                                       \
+        } else {                                                                                         \
+            shell_zpass_kernel<T, INDICATOR, NCV><<<(unsigned)(ntx * n), 256, sm_zy, st>>>(half, work, n, d2lo, \
+                                                                                             d2hi, plan, tw); \
+            PYSPEC_LAUNCH_CHECK();                                                                       \
+            shell_ypass_kernel<T, NCV><<<(unsigned)(ntx_active * n), 256, sm_zy, st>>>(work, n, d2hi,     \
+                                                                                       ntx_active, plan, tw); \
+            PYSPEC_LAUNCH_CHECK();                                                                       \
+        }                                                                                                \
         if constexpr (NCV > 0 && sizeof(T) == 4)                                                         \
             shell_xpass_reg_kernel<NCV, XR1(NCV), XR2(NCV)><<<nblk, 256, 0, st>>>(                           \
                 reinterpret_cast<const float2*>(work), xlim, reinterpret_cast<float*>(field), part,          \
