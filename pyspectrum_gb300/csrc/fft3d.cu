@@ -69,6 +69,74 @@ __global__ void __launch_bounds__(256) fft_strided_kernel(typename cplx_t<T>::ty
     }
 }
 
+// Register form of a pass for the common lengths N = R1 * R2: a CTA
+// transforms 8 lines in two radix stages with one padded shared-memory
+// exchange (as the shell line passes).  CONTIG: 8 consecutive contiguous lines
+// (the x axis; lanes run along the line, so loads are coalesced); otherwise 8
+// consecutive x columns of lines with element stride `row_stride` (the y and
+// z axes; lanes run across the columns).  In place.
+template <int NC, int R1, int R2>
+struct FftLineShape {
+    static constexpr int NB1 = NC / R1, NB2 = NC / R2;
+    static constexpr int NBM = NB1 > NB2 ? NB1 : NB2;
+    static constexpr int THREADS = 8 * NBM;
+    static constexpr int COLP = ((NC + NB1 + 13) / 16) * 16 + 2;   // padded line, == 2 (mod 16)
+};
+
+template <int NC, int R1, int R2, bool CONTIG>
+__global__ void __launch_bounds__(FftLineShape<NC, R1, R2>::THREADS)
+fft_line_kernel(float2* __restrict__ data, int64_t row_stride, int64_t outer_stride, int ntx, int sign) {
+    using S = FftLineShape<NC, R1, R2>;
+    constexpr int N = NC;
+    static_assert(R1 * R2 == N, "two radix stages");
+    __shared__ float2 tw[N];
+    __shared__ float2 buf[8 * S::COLP];
+    fill_twiddles<float>(tw, N, sign, threadIdx.x, blockDim.x);
+    int c, b;
+    float2* g;
+    int64_t es;                                  // element stride along the line
+    if constexpr (CONTIG) {
+        c = threadIdx.x / S::NBM;
+        b = threadIdx.x - c * S::NBM;
+        g = data + ((int64_t)blockIdx.x * 8 + c) * N;
+        es = 1;
+    } else {
+        c = threadIdx.x & 7;
+        b = threadIdx.x >> 3;
+        const int outer = blockIdx.x / ntx;
+        const int x0 = (blockIdx.x - outer * ntx) * 8;
+        g = data + (int64_t)outer * outer_stride + x0 + c;
+        es = row_stride;
+    }
+    __syncthreads();
+    float2* col = buf + c * S::COLP;
+    if (b < S::NB1) {
+        float2 v[R1];
+#pragma unroll
+        for (int r = 0; r < R1; ++r) v[r] = g[(int64_t)(b + r * S::NB1) * es];
+        small_dft<float, float2, R1>(v, sign);
+#pragma unroll
+        for (int r = 0; r < R1; ++r) col[b * (R1 + 1) + r] = v[r];    // element b*R1 + r
+    }
+    __syncthreads();
+    if (b < S::NB2) {
+        float2 v[R2];
+#pragma unroll
+        for (int r = 0; r < R2; ++r) {
+            const int p = b + r * S::NB2;                               // element index (< N)
+            const float2 u = col[p + p / R1];
+            v[r] = r == 0 || b == 0 ? u : cmul(u, tw[r * b]);
+        }
+        small_dft<float, float2, R2>(v, sign);
+#pragma unroll
+        for (int r = 0; r < R2; ++r) g[(int64_t)(b + r * S::NB2) * es] = v[r];
+    }
+}
+
+// radix split of the register passes per grid size (0: none)
+constexpr int FR1(int n) { return n == 360 ? 20 : n == 192 ? 16 : n == 256 ? 16 : 0; }
+constexpr int FR2(int n) { return n == 360 ? 18 : n == 192 ? 12 : n == 256 ? 16 : 1; }
+
 template <typename T>
 int fft3d_c2c_impl(typename cplx_t<T>::type* data, int n, int sign, cudaStream_t st) {
     using C = typename cplx_t<T>::type;
@@ -82,6 +150,20 @@ int fft3d_c2c_impl(typename cplx_t<T>::type* data, int n, int sign, cudaStream_t
     const int tx = tile_x<T>();
     const int ntx = (n + tx - 1) / tx;
     const size_t sm = sizeof(C) * ((size_t)n + 2 * (size_t)tx * n);
+#define PYSPEC_FFT3D_REG(NCV)                                                                             \
+    do {                                                                                                 \
+        using FS = FftLineShape<NCV, FR1(NCV), FR2(NCV)>;                                                \
+        float2* d = reinterpret_cast<float2*>(data);                                                     \
+        fft_line_kernel<NCV, FR1(NCV), FR2(NCV), true><<<(unsigned)(lines / 8), FS::THREADS, 0, st>>>(    \
+            d, 1, 0, 0, sign);                                                                           \
+        PYSPEC_LAUNCH_CHECK();                                                                           \
+        fft_line_kernel<NCV, FR1(NCV), FR2(NCV), false><<<(unsigned)(ntx * n), FS::THREADS, 0, st>>>(     \
+            d, n, (int64_t)n * n, ntx, sign);                                                            \
+        PYSPEC_LAUNCH_CHECK();                                                                           \
+        fft_line_kernel<NCV, FR1(NCV), FR2(NCV), false><<<(unsigned)(ntx * n), FS::THREADS, 0, st>>>(     \
+            d, (int64_t)n * n, n, ntx, sign);                                                            \
+        PYSPEC_LAUNCH_CHECK();                                                                           \
+    } while (0)
 #define PYSPEC_FFT3D_LAUNCH(NCV)                                                                          \
     do {                                                                                                 \
         PYSPEC_TRY(allow_smem((const void*)fft_contig_kernel<T, NCV>, sm_c));                            \
@@ -97,15 +179,16 @@ int fft3d_c2c_impl(typename cplx_t<T>::type* data, int n, int sign, cudaStream_t
     if constexpr (sizeof(T) == 4) {
         done = true;
         switch (n) {
-            case 192: PYSPEC_FFT3D_LAUNCH(192); break;
-            case 256: PYSPEC_FFT3D_LAUNCH(256); break;
-            case 360: PYSPEC_FFT3D_LAUNCH(360); break;
+            case 192: PYSPEC_FFT3D_REG(192); break;
+            case 256: PYSPEC_FFT3D_REG(256); break;
+            case 360: PYSPEC_FFT3D_REG(360); break;
             case 512: PYSPEC_FFT3D_LAUNCH(512); break;
             default: done = false;
         }
     }
     if (!done) PYSPEC_FFT3D_LAUNCH(0);
 #undef PYSPEC_FFT3D_LAUNCH
+#undef PYSPEC_FFT3D_REG
     count_launch(3);
     return PYSPEC_OK;
 }
