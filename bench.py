@@ -154,9 +154,22 @@ class ClockSampler:
                  "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+                 "--format=csv,noheader,nounits", "-lms", "20"], stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return self
+        # wait until nvidia-smi is sampling, then count only the samples taken
+        # from here on (the timed region starts when this returns)
+        self.skip = 0
+        t0 = time.time()
+        while time.time() - t0 < 10.0:
+            self.fh.flush()
+            with open(self.path) as f:
+                n = sum(1 for _ in f)
+            if n > 0:
+                self.skip = n
+                break
+            time.sleep(0.01)
         return self
 
     def __exit__(self, *a):
@@ -173,7 +186,9 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        for k, line in enumerate(open(self.path)):
+            if k < getattr(self, "skip", 0):
+                continue
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 8:
                 continue
