@@ -276,6 +276,33 @@ def run_gpu(args, rank, world, local_rank):
         if method == "bf16x3":
             results[method]["status_word"] = int(plan.ws_con[:4].view(torch.int32).item())
 
+    # timing comparator for the 3D FFT (cuFFT through torch.fft): the same
+    # unnormalised backward transform of the density grid, 5 repetitions each
+    fftcmp = None
+    try:
+        gtest = torch.complex(torch.randn((n, n, n), device=dev), torch.randn((n, n, n), device=dev))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        _lib.call("pyspec_fft3d_c2c", _lib.ptr(gtest), n, 1, _lib.stream_ptr())
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(5):
+            _lib.call("pyspec_fft3d_c2c", _lib.ptr(gtest), n, 1, _lib.stream_ptr())
+        e1.record()
+        torch.cuda.synchronize()
+        ours = e0.elapsed_time(e1) / 5
+        _ = torch.fft.ifftn(gtest, norm="forward")
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(5):
+            _ = torch.fft.ifftn(gtest, norm="forward")
+        e1.record()
+        torch.cuda.synchronize()
+        fftcmp = {"ours_ms": ours, "cufft_ms": e0.elapsed_time(e1) / 5,
+                  "transform": f"complex64 {n}^3 backward, unnormalised (cuFFT via torch.fft.ifftn, out of place)"}
+        del gtest
+    except Exception as exc:          # the comparator is informational only
+        fftcmp = {"error": str(exc)[:200]}
+
     # accuracy of the tensor-core form against the FP32 form on this workload
     step_fn(plans["bf16x3"])
     step_fn(plans["fp32"])
@@ -343,7 +370,7 @@ def run_gpu(args, rank, world, local_rank):
             "roofline": roofline, "cpu_baseline": cpu,
             "e2e": {"value": world * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "api": "pyspectrum_gb300.pyspectrum.Bk_periodic(pinned xyz)"},
-            "gpu_launches": main["gpu_launches"], "clocks": main["clocks"]}
+            "gpu_launches": main["gpu_launches"], "clocks": main["clocks"], "fft3d_comparator": fftcmp}
     print(json.dumps(line), flush=True)
 
 

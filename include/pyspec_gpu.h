@@ -104,6 +104,25 @@ int pyspec_fft3d_c2c(float *grid, int ngrid, int sign, void *stream);
 int pyspec_fcomb_periodic(const float *grid, int ngrid, double wsum, float *half, void *stream);
 
 /* ------------------------------------------------------------------------
+ * Survey (FKP) path -- pyspectrum.py:731-826 (FFT_survey_mono) and
+ * estimator.f:677-745 (fcomb_survey).
+ * pyspec_cast_positions: float64 (3, np) positions (element stride 1, row
+ *   stride dim_stride) and optional float64 weights -> float32, no clipping
+ *   (survey positions are centred on the origin; the assignment's offset of
+ *   N/2 cells moves them into the box).
+ * pyspec_fcomb_survey: as pyspec_fcomb_periodic with cf = 1/(6^3 * 4) (no
+ *   division by the weight sum; the FKP integrals normalise later).
+ * pyspec_combine_fields: out = a - alpha * b over n complex64 values, in
+ *   float32 without fused multiply-add (numpy's complex64 arithmetic), the
+ *   FKP field delta_g - alpha delta_r of pyspectrum.py:126.
+ * ---------------------------------------------------------------------- */
+int pyspec_cast_positions(const double *xyz, int64_t dim_stride, const double *w, int64_t np,
+                          float *xyz_out, float *w_out, void *stream);
+int pyspec_fcomb_survey(const float *grid, int ngrid, float *half, void *stream);
+int pyspec_combine_fields(const float *a, const float *b, double alpha, int64_t n, float *out,
+                          void *stream);
+
+/* ------------------------------------------------------------------------
  * reflect_delta -- pyspectrum.py:1134-1157: half grid -> full N^3 grid using
  * delta(-k) = conj(delta(k)); the seven Nyquist corners keep their real part.
  * half_from_full is the inverse used by _Bk_periodic when a caller passes a

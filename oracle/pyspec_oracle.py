@@ -324,6 +324,47 @@ def _Bk_periodic(delta_full, Nmax=40, Ncut=3, step=3, counts=None):
     return out
 
 
+def _B0_survey(delta_full, alpha, I12, I13, I22, I23, I33, Nmax=40, Ncut=3, step=3, counts=None):
+    """pyspectrum.py:137-282 (survey FKP bispectrum) in float64, triangles with
+    counts > 0 only (all arrays aligned)."""
+    n = delta_full.shape[0]
+    jmin = Ncut // step
+    F, p0k, nk = shell_fields(delta_full, step, jmin, Nmax)
+    p0k = p0k / I22 - (1.0 + alpha) * I12 / I22
+    if counts is None:
+        counts, _ = counts_Bk123(n, Nmax, Ncut, step)
+    res = {k: [] for k in ("i_k1", "i_k2", "i_k3", "p0k1", "p0k2", "p0k3", "b123", "q123", "counts")}
+    for i, j, l, fac in triangles(jmin, Nmax):
+        c = counts[i - 1, j - 1, l - 1]
+        if c > 0:
+            b = np.einsum("i,i,i", F[i].ravel(), F[j].ravel(), F[l].ravel()) / c
+            b -= (p0k[i - 1] + p0k[j - 1] + p0k[l - 1]) * I23 + (1.0 - alpha ** 2) * I13
+            b /= I33
+            res["i_k1"].append(i * step); res["i_k2"].append(j * step); res["i_k3"].append(l * step)
+            res["p0k1"].append(p0k[i - 1]); res["p0k2"].append(p0k[j - 1]); res["p0k3"].append(p0k[l - 1])
+            res["b123"].append(b)
+            res["q123"].append(b / (p0k[i - 1] * p0k[j - 1] + p0k[j - 1] * p0k[l - 1] + p0k[l - 1] * p0k[i - 1]))
+            res["counts"].append(c / (fac * float(n) ** 3))
+    return {k: np.array(v) for k, v in res.items()}
+
+
+def FFT_survey_mono(xyz, nb, w=None, P0_fkp=1e6, Lbox=2600.0, Ngrid=360):
+    """pyspectrum.py:773-826 from Cartesian positions (centred on the origin):
+    FKP weights, normalisation integrals, assignment with the N/2-cell offset,
+    backward FFT and fcomb_survey (fcomb_periodic with N = 1, estimator.f:686).
+    Returns (half grid, Ntot, I12, I13, I22, I23, I33)."""
+    npart = xyz.shape[1]
+    w = np.ones(npart) if w is None else np.array(w, dtype=np.float64)
+    Ntot = np.sum(w)
+    w = w * (1.0 / (1.0 + nb * P0_fkp))
+    I12, I13 = np.sum(w ** 2), np.sum(w ** 3)
+    I22, I23, I33 = np.sum(nb * w ** 2), np.sum(nb * w ** 3), np.sum(nb ** 2 * w ** 3)
+    xyzs = np.asarray(xyz, dtype=np.float32)
+    g = assign_quad(xyzs, w.astype(np.float32), np.float32(float(Ngrid) / Lbox), 0.5 * Ngrid, Ngrid)
+    G = fft_backward(g)
+    return fcomb_periodic(G, 1.0), Ntot, I12, I13, I22, I23, I33
+
+
 def Bk_periodic(xyz, w=None, Lbox=2600.0, Ngrid=360, step=3, Ncut=3, Nmax=40, counts=None):
     """pyspectrum.py:285-356 (the ``Ngrid == 360`` assertion at :332 is not kept)."""
     npart = np.asarray(xyz).shape[1]

@@ -44,6 +44,9 @@ SIGNATURES = {
     "pyspec_pk_monopole": (c_int, [_P, c_int, c_double, _P, _P]),
     "pyspec_pk_pbox_rsd": (c_int, [_P, c_int, c_int, c_int, c_int, c_int, _P, _P]),
     "pyspec_pk_rsd_python": (c_int, [_P, c_int, c_int, c_double, c_int, _P, _P]),
+    "pyspec_cast_positions": (c_int, [_P, c_i64, _P, c_i64, _P, _P, _P]),
+    "pyspec_fcomb_survey": (c_int, [_P, c_int, _P, _P]),
+    "pyspec_combine_fields": (c_int, [_P, _P, c_double, c_i64, _P, _P]),
 }
 
 CONTRACT_FP32 = 0

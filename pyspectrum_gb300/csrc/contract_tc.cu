@@ -59,7 +59,7 @@ constexpr int PWARPS = NPROD / 32;
 constexpr int MMA_WARP = PWARPS;
 constexpr int TMA_WARP = PWARPS + 1;
 constexpr int NTHREADS = NPROD + 64; // + the MMA warp + the copy warp
-constexpr int SEG = 64;              // chunks between accumulator drains (64: bf16x3 median error 4e-6 vs FP64; 128: 8e-6)
+constexpr int SEG = 32;              // chunks between accumulator drains (TMEM float32 accumulation length sets the error: 128 chunks gave a bf16x3 median error of 8e-6 vs FP64, 64 gave 4e-6)
 constexpr int MAXGROUPS = 8;
 constexpr int MAXTILES = 4;
 constexpr int MAXCOLS = 256;         // accumulator columns per group (+ 2 x 4 x 32 A columns <= 512)

@@ -7,9 +7,11 @@ namespace pyspec {
 // ---------------------------------------------------------------------------
 // pyspectrum.py:938-945 and util.py:72-74
 // ---------------------------------------------------------------------------
+// With clip == false (the survey path, pyspectrum.py:789-793) positions are
+// only cast to float32; lbox and the RSD shift are unused.
 __global__ void prepare_positions_kernel(const double* __restrict__ xyz, int64_t ds, const double* __restrict__ v,
                                          int64_t vs, int los, double rsd_factor, const double* __restrict__ w,
-                                         int64_t np, double lbox, float* __restrict__ out,
+                                         int64_t np, double lbox, bool clip, float* __restrict__ out,
                                          float* __restrict__ wout) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
@@ -17,12 +19,14 @@ __global__ void prepare_positions_kernel(const double* __restrict__ xyz, int64_t
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         double x = xyz[d * ds + i];
-        if (v != nullptr && d == los) {
-            // applyRSD: (x + f*v + L) mod L, numpy's floored modulo
-            x = x + (rsd_factor * v[d * vs + i] + lbox);
-            x = x - floor(x / lbox) * lbox;
+        if (clip) {
+            if (v != nullptr && d == los) {
+                // applyRSD: (x + f*v + L) mod L, numpy's floored modulo
+                x = x + (rsd_factor * v[d * vs + i] + lbox);
+                x = x - floor(x / lbox) * lbox;
+            }
+            x = fmin(fmax(x, 0.0), hi);
         }
-        x = fmin(fmax(x, 0.0), hi);
         out[d * np + i] = (float)x;
     }
     if (wout != nullptr) wout[i] = w ? (float)w[i] : 1.0f;
@@ -228,7 +232,20 @@ extern "C" int pyspec_prepare_positions(const double* xyz, int64_t dim_stride, c
     PYSPEC_CHECK_ARG(vxyz == nullptr || (los >= 0 && los < 3), "los must be 0, 1 or 2");
     const int bs = 256;
     prepare_positions_kernel<<<(unsigned)((np + bs - 1) / bs), bs, 0, as_stream(stream)>>>(
-        xyz, dim_stride, vxyz, vdim_stride, los, rsd_factor, w, np, lbox, xyz_out, w_out);
+        xyz, dim_stride, vxyz, vdim_stride, los, rsd_factor, w, np, lbox, true, xyz_out, w_out);
+    PYSPEC_LAUNCH_CHECK();
+    count_launch();
+    return PYSPEC_OK;
+}
+
+extern "C" int pyspec_cast_positions(const double* xyz, int64_t dim_stride, const double* w, int64_t np,
+                                     float* xyz_out, float* w_out, void* stream) {
+    PYSPEC_CHECK_ARG(np >= 0, "np < 0");
+    if (np == 0) return PYSPEC_OK;
+    PYSPEC_CHECK_ARG(xyz && xyz_out, "NULL position pointer");
+    const int bs = 256;
+    prepare_positions_kernel<<<(unsigned)((np + bs - 1) / bs), bs, 0, as_stream(stream)>>>(
+        xyz, dim_stride, nullptr, 0, 0, 0.0, w, np, 1.0, false, xyz_out, w_out);
     PYSPEC_LAUNCH_CHECK();
     count_launch();
     return PYSPEC_OK;
@@ -248,17 +265,52 @@ extern "C" int pyspec_assign_pcs_interlaced(const float* xyz, const float* w, in
     return PYSPEC_OK;
 }
 
+static int fcomb_launch(const float* grid, int ngrid, float cf, float* half, void* stream) {
+    const int64_t l = ngrid / 2 + 1;
+    const int64_t nt = l * l * l;
+    const int bs = 128;
+    fcomb_kernel<<<(unsigned)((nt + bs - 1) / bs), bs, 0, as_stream(stream)>>>(
+        reinterpret_cast<const float2*>(grid), ngrid, cf, reinterpret_cast<float2*>(half));
+    PYSPEC_LAUNCH_CHECK();
+    count_launch();
+    return PYSPEC_OK;
+}
+
 extern "C" int pyspec_fcomb_periodic(const float* grid, int ngrid, double wsum, float* half, void* stream) {
     PYSPEC_CHECK_ARG(grid && half, "NULL pointer");
     PYSPEC_CHECK_ARG(ngrid >= 2 && ngrid % 2 == 0, "ngrid=%d must be even", ngrid);
     PYSPEC_CHECK_ARG(wsum != 0.0, "sum of weights is zero");
-    const int64_t l = ngrid / 2 + 1;
-    const int64_t nt = l * l * l;
     // estimator.f:615: cf = 1/(6^3 * 4 * N), single precision
-    const float cf = (float)(1.0 / (216.0 * 4.0 * (double)(float)wsum));
-    const int bs = 128;
-    fcomb_kernel<<<(unsigned)((nt + bs - 1) / bs), bs, 0, as_stream(stream)>>>(
-        reinterpret_cast<const float2*>(grid), ngrid, cf, reinterpret_cast<float2*>(half));
+    return fcomb_launch(grid, ngrid, (float)(1.0 / (216.0 * 4.0 * (double)(float)wsum)), half, stream);
+}
+
+extern "C" int pyspec_fcomb_survey(const float* grid, int ngrid, float* half, void* stream) {
+    PYSPEC_CHECK_ARG(grid && half, "NULL pointer");
+    PYSPEC_CHECK_ARG(ngrid >= 2 && ngrid % 2 == 0, "ngrid=%d must be even", ngrid);
+    // estimator.f:686: cf = 1/(6^3 * 4), the FKP normalisation is applied later
+    return fcomb_launch(grid, ngrid, (float)(1.0 / (216.0 * 4.0)), half, stream);
+}
+
+// out = a - alpha * b over n complex64 values (the FKP field F = n_g - alpha n_r
+// in Fourier space, pyspectrum.py:126)
+__global__ void axpy_kernel(const float2* __restrict__ a, const float2* __restrict__ b, double alpha, int64_t n,
+                            float2* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float2 x = a[i], y = b[i];
+    const float al = (float)alpha;        // numpy: complex64 field times a Python float
+    out[i] = make_float2(__fsub_rn(x.x, __fmul_rn(al, y.x)), __fsub_rn(x.y, __fmul_rn(al, y.y)));
+}
+
+extern "C" int pyspec_combine_fields(const float* a, const float* b, double alpha, int64_t n, float* out,
+                                     void* stream) {
+    PYSPEC_CHECK_ARG(a && b && out, "NULL pointer");
+    PYSPEC_CHECK_ARG(n >= 0, "n < 0");
+    if (n == 0) return PYSPEC_OK;
+    const int bs = 256;
+    axpy_kernel<<<(unsigned)((n + bs - 1) / bs), bs, 0, as_stream(stream)>>>(
+        reinterpret_cast<const float2*>(a), reinterpret_cast<const float2*>(b), alpha, n,
+        reinterpret_cast<float2*>(out));
     PYSPEC_LAUNCH_CHECK();
     count_launch();
     return PYSPEC_OK;

@@ -343,14 +343,21 @@ __global__ void __launch_bounds__(256) shell_xpass_kernel(const typename cplx_t<
 
 // x rows for the common grid sizes, with the half-length FFT of H = R1*R2
 // points done in registers: a warp transforms two rows at a time (16 lanes
-// per row).  Stage 1 loads its inputs straight from the work grid, forms
+// per row).  The next pair of rows is copied into a per-warp staging buffer
+// with cp.async while the current pair is transformed, so the row loads are
+// always in flight.  Stage 1 reads its inputs from the staging buffer, forms
 // Z[k] (the C2R packing above) and applies radix-R1 butterflies; the outputs
 // cross lanes once through a padded per-row buffer in shared memory (one pad
 // element per R1, so neither side has bank conflicts); stage 2 applies the
 // twiddles and radix-R2 butterflies and stores the row of F directly.  No
 // block-wide barrier: each warp only synchronises with itself.
 template <int NC, int R1, int R2>
-__global__ void __launch_bounds__(256, 4) shell_xpass_reg_kernel(const float2* __restrict__ work, int xlim,
+__host__ __device__ constexpr size_t xpass_reg_smem() {
+    return (size_t)8 * 2 * 2 * work_stride<float2>(NC) * sizeof(float2);   // 8 warps x 2 stages x 2 rows
+}
+
+template <int NC, int R1, int R2>
+__global__ void __launch_bounds__(256, 3) shell_xpass_reg_kernel(const float2* __restrict__ work, int xlim,
                                                               float* __restrict__ field, double* __restrict__ part,
                                                               const float2* __restrict__ twg) {
     constexpr int N = NC, H = N / 2, WS = work_stride<float2>(N);
@@ -360,6 +367,7 @@ __global__ void __launch_bounds__(256, 4) shell_xpass_reg_kernel(const float2* _
     __shared__ float2 twH[H];                    // exp(-2 pi i m / H)
     __shared__ float2 rowbuf[8][2][PADH];
     __shared__ double red[8];
+    extern __shared__ __align__(16) float2 stage_all[];   // [warp][stage][row][WS]
     for (int i = threadIdx.x; i < H; i += blockDim.x) {
         twN[i] = twg[i];
         twH[i] = twg[N + i];
@@ -368,12 +376,33 @@ __global__ void __launch_bounds__(256, 4) shell_xpass_reg_kernel(const float2* _
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int sub = lane >> 4, t = lane & 15;
     float2* buf = rowbuf[warp][sub];
+    float2* stg = stage_all + (size_t)warp * 2 * 2 * WS;
     const int64_t nrows = (int64_t)N * N;        // even: rows come in pairs
     const int64_t nw = (int64_t)gridDim.x * 8;
+    // 16-byte pieces of a row holding its first xlim elements
+    const int npiece = (xlim + 1) / 2;
+    // copy the two rows starting at r0 into stage sb (every lane commits one group)
+    auto issue = [&](int64_t r0, int sb) {
+        if (r0 < nrows) {
+            for (int q = lane; q < 2 * npiece; q += 32) {
+                const int rr = q >= npiece, pc = q - rr * npiece;
+                const float2* src = work + (r0 + rr) * WS + 2 * pc;
+                const uint32_t dst = (uint32_t)__cvta_generic_to_shared(stg + ((size_t)sb * 2 + rr) * WS + 2 * pc);
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" :: "r"(dst), "l"(src) : "memory");
+            }
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
     float local = 0.f;
-    for (int64_t r0 = ((int64_t)blockIdx.x * 8 + warp) * 2; r0 < nrows; r0 += nw * 2) {
+    int sb = 0;
+    int64_t r0 = ((int64_t)blockIdx.x * 8 + warp) * 2;
+    issue(r0, 0);
+    for (; r0 < nrows; r0 += nw * 2, sb ^= 1) {
+        issue(r0 + nw * 2, sb ^ 1);
+        asm volatile("cp.async.wait_group 1;" ::: "memory");
+        __syncwarp();                         // every lane's pieces of this pair have landed
         const int64_t row = r0 + sub;
-        const float2* X = work + row * WS;
+        const float2* X = stg + ((size_t)sb * 2 + sub) * WS;
         if (t < R2) {
             float2 v[R1];
 #pragma unroll
@@ -407,8 +436,9 @@ __global__ void __launch_bounds__(256, 4) shell_xpass_reg_kernel(const float2* _
                 local += v[r].x * v[r].x + v[r].y * v[r].y;
             }
         }
-        __syncwarp();                         // buf is rewritten for the next pair
+        __syncwarp();                         // buf and this stage are rewritten later
     }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
     double acc = (double)local;
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) red[warp] = acc;
@@ -443,7 +473,7 @@ static int xpass_ctas(int n) {
     int sms = 152, dev = 0;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int64_t blocks = ((int64_t)n * n + xpass_rows(n) - 1) / xpass_rows(n);
-    return (int)std::min<int64_t>(blocks, (int64_t)sms * 4);
+    return (int)std::min<int64_t>(blocks, (int64_t)sms * 3);
 }
 
 template <typename T>
@@ -491,6 +521,10 @@ int shell_one_impl(const typename cplx_t<T>::type* half, int n, int step, int j,
         PYSPEC_TRY(allow_smem((const void*)shell_zpass_kernel<T, INDICATOR, NCV>, sm_zy));               \
         PYSPEC_TRY(allow_smem((const void*)shell_ypass_kernel<T, NCV>, sm_zy));                          \
         PYSPEC_TRY(allow_smem((const void*)shell_xpass_kernel<T, NCV>, sm_x));                           \
+        if constexpr (NCV > 0 && sizeof(T) == 4)                                                         \
+            PYSPEC_CUDA(cudaFuncSetAttribute((const void*)shell_xpass_reg_kernel<NCV, XR1(NCV), XR2(NCV)>,  \
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,                \
+                                             (int)xpass_reg_smem<NCV, XR1(NCV), XR2(NCV)>()));           \
         if constexpr (LR1(NCV) > 0 && sizeof(T) == 4) {                                                   \
             using LS = LinePassShape<NCV, LR1(NCV), LR2(NCV)>;                                            \
             shell_line_pass_kernel<NCV, LR1(NCV), LR2(NCV), true, INDICATOR>                               \
@@ -511,7 +545,8 @@ int shell_one_impl(const typename cplx_t<T>::type* half, int n, int step, int j,
             PYSPEC_LAUNCH_CHECK();                                                                       \
         }                                                                                                \
         if constexpr (NCV > 0 && sizeof(T) == 4)                                                         \
-            shell_xpass_reg_kernel<NCV, XR1(NCV), XR2(NCV)><<<nblk, 256, 0, st>>>(                           \
+            shell_xpass_reg_kernel<NCV, XR1(NCV), XR2(NCV)><<<nblk, 256,                                    \
+                                                               xpass_reg_smem<NCV, XR1(NCV), XR2(NCV)>(), st>>>( \
                 reinterpret_cast<const float2*>(work), xlim, reinterpret_cast<float*>(field), part,          \
                 reinterpret_cast<const float2*>(tw));                                                    \
         else                                                                                             \

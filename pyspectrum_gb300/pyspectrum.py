@@ -29,11 +29,12 @@ import torch
 
 from . import core
 from .batch import Bk_periodic_batch  # noqa: F401  (many boxes per call; no reference counterpart)
+from .survey import B0_survey, FFT_survey_mono, _B0_survey  # noqa: F401  (pyspectrum.py:13-282, 731-826)
 from .util import applyRSD  # noqa: F401  (re-exported as the tests of the reference expect)
 
 __all__ = ["FFT_periodic", "FFTperiodic", "reflect_delta", "Pk_periodic", "Pk_periodic_rsd", "_Pk_periodic_rsd",
            "Bk_periodic", "_Bk_periodic", "Bk_periodic_rsd", "_counts_Bk123", "_counts_Bk123_f77",
-           "applyRSD", "Bk_periodic_batch"]
+           "applyRSD", "Bk_periodic_batch", "B0_survey", "_B0_survey", "FFT_survey_mono"]
 
 
 def _np_weights(w, n):
@@ -52,8 +53,14 @@ def _half_from_numpy(delt, device=None) -> torch.Tensor:
 
 
 def _delta_half_device(xyz, w, Lbox, Ngrid, vel=None, los=2, rsd_factor=0.0, device=None):
-    dev = core._dev(device)
     npart = np.asarray(xyz).shape[1] if not torch.is_tensor(xyz) else xyz.shape[1]
+    if npart == 0:
+        raise ValueError("empty catalogue: the density contrast needs at least one object")
+    if int(Ngrid) < 4 or int(Ngrid) % 2:
+        raise ValueError("Ngrid must be even and >= 4")
+    if w is not None and float(np.sum(np.asarray(w, dtype=np.float64))) == 0.0:
+        raise ValueError("the weights sum to zero (the density is normalised by their sum)")
+    dev = core._dev(device)
     w_np = _np_weights(w, npart)
     xyz_d = core.positions_to_device(xyz, dev)
     w_d = None if w is None else torch.as_tensor(w_np, device=dev)

@@ -2,7 +2,7 @@
 
 Run once in a checkout that has the reference source tree (read-only is fine):
 
-    PYSPEC_REFERENCE=<path to pySpectrum checkout> python tests/golden/make_golden.py [pk_rsd_python]
+    PYSPEC_REFERENCE=<path to pySpectrum checkout> python tests/golden/make_golden.py [pk_rsd_python | b0_survey]
 
 What it produces (all small, committed):
 
@@ -18,6 +18,8 @@ What it produces (all small, committed):
 * ``ref_fft_small.npz`` -- the reference's ``_FFT`` (de-interleave +
   unnormalised backward FFT) on a seeded interlaced grid.
 * ``ref_rsd.npz`` -- the reference's ``util.applyRSD`` on fixture halos.
+* ``ref_b0_survey.npz`` -- the reference's ``_B0_survey`` (survey FKP
+  bispectrum from a full delta(k) and normalisation integrals) at N = 16, 24.
 * ``ref_pk_rsd_python.npz`` -- the reference's ``_Pk_periodic_rsd`` with
   ``code='python'`` (its numpy (k, mu) binning) on seeded full delta(k)
   grids at N = 16, 24 for every line of sight.
@@ -201,6 +203,25 @@ def pk_rsd_python_goldens(ref):
     np.savez_compressed(os.path.join(HERE, "ref_pk_rsd_python.npz"), **out)
 
 
+def b0_survey_goldens(ref, tmp):
+    ref.dat_dir = lambda: tmp            # the count cache is written here
+    cases = [(16, 1, 1, 6), (24, 2, 2, 6)]
+    out = {"cases": np.array(cases)}
+    for n, step, ncut, nmax in cases:
+        rng = np.random.default_rng(700 + n)
+        full = (np.fft.fftn(rng.standard_normal((n, n, n))) / n ** 1.5).astype(np.complex64)
+        ints = rng.uniform(0.5, 2.0, size=5)
+        alpha = 0.05
+        res = ref._B0_survey(full, alpha, *ints, Nmax=nmax, Ncut=ncut, step=step, fft="pyfftw")
+        tag = f"n{n}_s{step}_c{ncut}_m{nmax}"
+        out[tag + "_delta"] = full
+        out[tag + "_ints"] = ints
+        out[tag + "_alpha"] = np.array(alpha)
+        for k, v in res.items():
+            out[tag + "_" + k] = np.asarray(v)
+    np.savez_compressed(os.path.join(HERE, "ref_b0_survey.npz"), **out)
+
+
 def main():
     FlatLambdaCDM = _install_stubs()
     sys.path.insert(0, REF)
@@ -209,7 +230,13 @@ def main():
     if sys.argv[1:] == ["pk_rsd_python"]:           # only this fixture
         pk_rsd_python_goldens(ref)
         return
+    if sys.argv[1:] == ["b0_survey"]:               # only this fixture
+        with tempfile.TemporaryDirectory() as tmp:
+            b0_survey_goldens(ref, tmp)
+        return
     pk_rsd_python_goldens(ref)
+    with tempfile.TemporaryDirectory() as tmp:
+        b0_survey_goldens(ref, tmp)
     counts_goldens()
     with tempfile.TemporaryDirectory() as tmp:
         bk_goldens(ref, tmp)

@@ -5,6 +5,7 @@ import ctypes
 import os
 import re
 
+import numpy as np
 import pytest
 
 from pyspectrum_gb300 import _build, _lib
@@ -67,3 +68,28 @@ def test_workspace_too_small_reported():
                                  ctypes.c_void_p(256), 16, None)
     assert rc == -4
     assert "workspace" in _lib.last_error()
+
+
+@pytest.mark.parametrize("call", [
+    lambda l: l.pyspec_fcomb_periodic(ctypes.c_void_p(16), 16, 0.0, ctypes.c_void_p(16), None),
+    lambda l: l.pyspec_pk_rsd_python(ctypes.c_void_p(16), 16, 3, 100.0, 5, ctypes.c_void_p(16), None),
+    lambda l: l.pyspec_pk_rsd_python(ctypes.c_void_p(16), 16, 2, 100.0, 0, ctypes.c_void_p(16), None),
+    lambda l: l.pyspec_pk_rsd_python(ctypes.c_void_p(16), 15, 2, 100.0, 4, ctypes.c_void_p(16), None),
+    lambda l: l.pyspec_bk_contract_noalloc(None, 16, 4, None, 1, None, None),
+    lambda l: l.pyspec_bk_contract_noalloc(ctypes.c_void_p(16), 16, 0, ctypes.c_void_p(16), 1,
+                                           ctypes.c_void_p(16), None),
+])
+def test_more_invalid_arguments(call):
+    lib = _lib.load()
+    assert call(lib) == -1
+    assert _lib.last_error() != ""
+
+
+def test_python_layer_rejects_degenerate_catalogues():
+    from pyspectrum_gb300 import pyspectrum as P
+    with pytest.raises(ValueError, match="empty"):
+        P.Bk_periodic(np.zeros((3, 0)), Lbox=100.0, Ngrid=16)
+    with pytest.raises(ValueError, match="sum to zero"):
+        P.Pk_periodic(np.ones((3, 4)), w=np.zeros(4), Lbox=100.0, Ngrid=16)
+    with pytest.raises(ValueError, match="even"):
+        P.FFT_periodic(np.ones((3, 4)), Lbox=100.0, Ngrid=15)

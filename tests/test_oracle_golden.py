@@ -145,3 +145,19 @@ def test_pk_rsd_python_matches_reference(golden):
             else:
                 # the reference sums float32 |delta|^2 in float32 (np.sum)
                 np.testing.assert_allclose(v, r, rtol=2e-6, atol=1e-9 * np.abs(r).max(), err_msg=tag + name)
+
+
+def test_b0_survey_oracle_matches_reference(golden):
+    """_B0_survey (pyspectrum.py:137-282) restated, against the reference's own
+    output on seeded FKP fields."""
+    g = golden("ref_b0_survey.npz")
+    for n, step, ncut, nmax in g["cases"]:
+        tag = f"n{n}_s{step}_c{ncut}_m{nmax}"
+        ints = g[tag + "_ints"]
+        got = O._B0_survey(g[tag + "_delta"].astype(np.complex128), float(g[tag + "_alpha"]), *ints,
+                           Nmax=int(nmax), Ncut=int(ncut), step=int(step))
+        for k in ("i_k1", "i_k2", "i_k3"):
+            np.testing.assert_array_equal(got[k], g[tag + "_" + k])
+        for k in ("p0k1", "b123", "q123", "counts"):
+            r = g[tag + "_" + k]
+            np.testing.assert_allclose(got[k], r, rtol=1e-5, atol=1e-6 * np.abs(r).max(), err_msg=tag + k)
