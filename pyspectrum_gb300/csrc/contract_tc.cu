@@ -253,12 +253,12 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
     if (tid == 0) {
         abort_flag = 0;
         for (int s = 0; s < NSTAGE; ++s) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_full[s])), "r"(PWARPS));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_full[s])), "r"(PWARPS / 2));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_empty[s])), "r"(1));
         }
         for (int b = 0; b < NFBUF; ++b) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_ffull[b])), "r"(1));
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_fempty[b])), "r"(PWARPS));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_fempty[b])), "r"(PWARPS / 2));
         }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_seg)), "r"(1));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_drained)), "r"(PWARPS));
@@ -280,34 +280,95 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
 
     if (warp < PWARPS) {
         // ================= producers =================
+        // Two groups of 8 warps take alternate chunks (group g: chunks c with
+        // c % 2 == g, A / B stage g), so one group's shared-memory loads overlap
+        // the other's arithmetic.  Warp w of group g owns TMEM lane quarter w % 4
+        // of tiles (w % 8) / 4 and (w % 8) / 4 + 2: one pair row per tile.
         const int rows = G.rows;
         const int nsh = P.nshell;
-        const int mytile = warp >> 2;                 // warp-uniform
-        const bool tile_on = mytile < G.ntiles;
-        const int row = 128 * mytile + 32 * q + lane;
-        const bool row_on = tile_on && row < rows && pij[4 * row] >= 0;
-        const int ri = row_on ? (pij[4 * row] & 0xff) : 0;
-        const int rj = row_on ? (pij[4 * row] >> 8) : 0;
-        // B writer: shell r, k-group g (voxels 8g..8g+7)
-        int ub_r = -1, ub_g = 0;
-        if (tid < nsh * 4) {
-            ub_g = (tid >= nsh) + (tid >= 2 * nsh) + (tid >= 3 * nsh);
-            ub_r = tid - ub_g * nsh;
+        const int grp = warp >> 3;
+        const int gtid = tid & 255;                   // thread index within the group
+        int ri[2], rj[2];
+        bool ton[2], ron[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int t = ((warp & 7) >> 2) + 2 * u;  // warp-uniform
+            const int row = 128 * t + 32 * q + lane;
+            ton[u] = t < G.ntiles;
+            ron[u] = ton[u] && row < rows && pij[4 * row] >= 0;
+            ri[u] = ron[u] ? (pij[4 * row] & 0xff) : 0;
+            rj[u] = ron[u] ? (pij[4 * row] >> 8) : 0;
         }
+        const int tl[2] = {(warp & 7) >> 2, ((warp & 7) >> 2) + 2};
+        // B writer: shell r, k-group g (voxels 8g..8g+7); 4 nshell <= 256 threads per group
+        int ub_r = -1, ub_g = 0;
+        if (gtid < nsh * 4) {
+            ub_g = (gtid >= nsh) + (gtid >= 2 * nsh) + (gtid >= 3 * nsh);
+            ub_r = gtid - ub_g * nsh;
+        }
+        const int nseg = (nch + SEG - 1) / SEG;
         int seg_count = 0;
-        for (int c = 0; c < nch; ++c) {
-            if (__any_sync(0xffffffffu, abort_flag != 0)) break;   // warp-uniform exit
-            const int s = c & 1;
+        bool failed = false;
+        // drain the accumulators of segment seg_count (all warps of both groups)
+        auto drain = [&]() -> bool {
+            if (!warp_wait(smem_u32(&bar_seg), seg_count & 1)) return false;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            // the four warps of this lane quarter take 32-column groups
+            // (hi and lo columns of 16 shells) round-robin; one thread adds
+            // the hi and lo parts of a (row, shell) and updates its slot
+            for (int cg = 32 * ((warp >> 2) & 3); cg < C; cg += 128) {
+                uint32_t d[32];
+                tmem_ld8(lane_base + (uint32_t)cg, d);
+                tmem_ld8(lane_base + (uint32_t)cg + 8u, d + 8);
+                tmem_ld8(lane_base + (uint32_t)cg + 16u, d + 16);
+                tmem_ld8(lane_base + (uint32_t)cg + 24u, d + 24);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                int t = 0;
+                while (t + 1 < G.ntiles && cg >= G.tile_col[t + 1]) ++t;
+                if (cg >= G.tile_col[t] + 2 * G.tile_n[t]) continue;
+                const int drow = 128 * t + 32 * q + lane;
+                // this row's columns l in [lmin, lmax] own slots base + (l - lmin)
+                const short4 pr = drow < rows ? *reinterpret_cast<const short4*>(&pij[4 * drow])
+                                              : make_short4(-1, 0, -1, 0);
+                const int sh0 = col_shell(cg - G.tile_col[t]);
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                    const int l = sh0 + e;
+                    if (pr.x < 0 || l < pr.y || l > pr.z) continue;
+                    const int slot = pr.w + (l - pr.y);
+                    const float v = __uint_as_float(d[e]) + __uint_as_float(d[16 + e]);
+                    const float2 a = acc[slot];
+                    const float y = v - a.y;
+                    const float sum = a.x + y;
+                    acc[slot] = make_float2(sum, (sum - a.x) - y);
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&bar_drained));
+            ++seg_count;
+            return true;
+        };
+        for (int c = grp; c < nch; c += 2) {
+            if (__any_sync(0xffffffffu, abort_flag != 0)) { failed = true; break; }   // warp-uniform exit
+            // segments that ended before this chunk are drained first
+            while (seg_count < nseg && (seg_count + 1) * SEG - 1 < c) {
+                if (!drain()) { atomicExch(P.err, 2); abort_flag = 1; failed = true; break; }
+            }
+            if (failed) break;
+            const int s = grp;                        // == c & 1
             const int b = c % NFBUF;
             if (!warp_wait(smem_u32(&bar_ffull[b]), (uint32_t)(c / NFBUF) & 1u)) {
                 atomicExch(P.err, 1);
                 abort_flag = 1;
+                failed = true;
                 break;
             }
             if (c >= NSTAGE) {
                 if (!warp_wait(smem_u32(&bar_empty[s]), ((c - NSTAGE) >> 1) & 1)) {
                     atomicExch(P.err, 1);
                     abort_flag = 1;
+                    failed = true;
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -322,17 +383,19 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
                                      make_float2(e.z, e.w)};
                 split_store8(x, Bst + op_off(brow(ub_r, 0), ub_g), Bst + op_off(brow(ub_r, 1), ub_g));
             }
-            // A operand: this lane's pair products, straight into TMEM
-            if (tile_on) {
+            // A operand: this lane's pair products of both tiles, straight into TMEM
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                if (!ton[u]) continue;                // warp-uniform
 #pragma unroll
                 for (int ks = 0; ks < KC / 16; ++ks) {
                     uint32_t h[8], l[8];
 #pragma unroll
                     for (int g = 0; g < 4; ++g) {
                         float4 a = make_float4(0.f, 0.f, 0.f, 0.f), e = a;
-                        if (row_on) {
-                            a = *reinterpret_cast<const float4*>(F + fchunk(ri, 4 * ks + g));
-                            e = *reinterpret_cast<const float4*>(F + fchunk(rj, 4 * ks + g));
+                        if (ron[u]) {
+                            a = *reinterpret_cast<const float4*>(F + fchunk(ri[u], 4 * ks + g));
+                            e = *reinterpret_cast<const float4*>(F + fchunk(rj[u], 4 * ks + g));
                         }
                         const float2 p0 = mul2(make_float2(a.x, a.y), make_float2(e.x, e.y));
                         const float2 p1 = mul2(make_float2(a.z, a.w), make_float2(e.z, e.w));
@@ -345,64 +408,24 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
                         l[2 * g] = pack_bf16x2(l0.x, l0.y);
                         l[2 * g + 1] = pack_bf16x2(l1.x, l1.y);
                     }
-                    tmem_st8(lane_base + acol(s, mytile, ks), h);
-                    tmem_st8(lane_base + acol(s, mytile, ks) + 8u, l);
+                    tmem_st8(lane_base + acol(s, tl[u], ks), h);
+                    tmem_st8(lane_base + acol(s, tl[u], ks) + 8u, l);
                 }
-                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
             }
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            // one arrive per warp (the barriers count warps): the lanes' writes
-            // and reads are ordered before lane 0's release by the warp barrier
+            // one arrive per warp (the barriers count the 8 warps of a group):
+            // the lanes' writes and reads are ordered before lane 0's release
             __syncwarp();
             if (lane == 0) {
                 mbar_arrive(smem_u32(&bar_full[s]));
                 mbar_arrive(smem_u32(&bar_fempty[b]));
             }
-            // drain after the last chunk of every segment: add the segment's
-            // accumulators into the Kahan sums in shared memory
-            if ((c + 1) % SEG == 0 || c + 1 == nch) {
-                if (!warp_wait(smem_u32(&bar_seg), seg_count & 1)) {
-                    atomicExch(P.err, 2);
-                    abort_flag = 1;
-                    break;
-                }
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                // the four warps of this lane quarter take 32-column groups
-                // (hi and lo columns of 16 shells) round-robin; one thread adds
-                // the hi and lo parts of a (row, shell) and updates its slot
-                for (int cg = 32 * (warp >> 2); cg < C; cg += 128) {
-                    uint32_t d[32];
-                    tmem_ld8(lane_base + (uint32_t)cg, d);
-                    tmem_ld8(lane_base + (uint32_t)cg + 8u, d + 8);
-                    tmem_ld8(lane_base + (uint32_t)cg + 16u, d + 16);
-                    tmem_ld8(lane_base + (uint32_t)cg + 24u, d + 24);
-                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                    int t = 0;
-                    while (t + 1 < G.ntiles && cg >= G.tile_col[t + 1]) ++t;
-                    if (cg >= G.tile_col[t] + 2 * G.tile_n[t]) continue;
-                    const int drow = 128 * t + 32 * q + lane;
-                    // this row's columns l in [lmin, lmax] own slots base + (l - lmin)
-                    const short4 pr = drow < rows ? *reinterpret_cast<const short4*>(&pij[4 * drow])
-                                                  : make_short4(-1, 0, -1, 0);
-                    const int sh0 = col_shell(cg - G.tile_col[t]);
-#pragma unroll
-                    for (int e = 0; e < 16; ++e) {
-                        const int l = sh0 + e;
-                        if (pr.x < 0 || l < pr.y || l > pr.z) continue;
-                        const int slot = pr.w + (l - pr.y);
-                        const float v = __uint_as_float(d[e]) + __uint_as_float(d[16 + e]);
-                        const float2 a = acc[slot];
-                        const float y = v - a.y;
-                        const float sum = a.x + y;
-                        acc[slot] = make_float2(sum, (sum - a.x) - y);
-                    }
-                }
-                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-                __syncwarp();
-                if (lane == 0) mbar_arrive(smem_u32(&bar_drained));
-                ++seg_count;
-            }
+        }
+        // the remaining segments (the last one ends with the last chunk)
+        while (!failed && seg_count < nseg) {
+            if (!drain()) { atomicExch(P.err, 2); abort_flag = 1; break; }
         }
     } else if (warp == MMA_WARP) {
         if (lane == 0) {
