@@ -204,6 +204,55 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+FP64_SHELLS = (1, 2, 3, 5, 8, 13, 20, 27, 34, 40)
+
+
+def fp64_error(half, plans):
+    """Error of both contraction forms against float64 sums on the bench box:
+    the shell fields of FP64_SHELLS rebuilt from the same delta(k) with
+    complex128 FFTs (scipy, all host cores) and the triangles among those
+    shells summed in float64.  Reports, per form, the median and maximum
+    |dB/B|, the maximum over triangles with condition number
+    sum|F_iF_jF_l| / |sum F_iF_jF_l| < 1e3, and the maximum error normalised by
+    sum|F_iF_jF_l|."""
+    import scipy.fft as sfft
+    import torch
+    from pyspectrum_gb300 import core
+    t0 = time.perf_counter()
+    bsums = {}
+    for name, pl in plans.items():          # both forms from this same delta(k)
+        pl.shells(half)
+        pl.contract()
+        bsums[name] = pl.bsum.cpu().numpy()
+    plan = plans["bf16x3"]
+    n, step = plan.n, plan.step
+    delta = core.reflect_half(half).cpu().numpy().astype(np.complex128)
+    torch.cuda.empty_cache()
+    a = np.minimum(np.arange(n), n - np.arange(n)).astype(np.int64)
+    d2 = a[:, None, None] ** 2 + a[None, :, None] ** 2 + a[None, None, :] ** 2
+    irk = np.floor(np.sqrt(d2.astype(np.float64)) / step + 0.5).astype(np.int64)
+    irk -= ((2 * irk - 1) ** 2 * step * step > 4 * d2) & (irk > 0)        # exact integer shell rule
+    irk += (2 * irk + 1) ** 2 * step * step <= 4 * d2
+    F = {j: np.real(sfft.fftn(np.where(irk == j, delta, 0), workers=-1)).ravel() for j in FP64_SHELLS}
+    del delta, irk, d2
+    loop = plan.tri_np
+    sel = [t for t in range(loop.shape[1]) if all(int(v) in F for v in loop[:, t])]
+    exact = np.empty(len(sel))
+    absum = np.empty(len(sel))
+    for k, t in enumerate(sel):
+        prod = F[int(loop[0, t])] * F[int(loop[1, t])] * F[int(loop[2, t])]
+        exact[k], absum[k] = prod.sum(), np.abs(prod).sum()
+    cond = absum / np.abs(exact)
+    out = {"triangles": len(sel), "shells": list(FP64_SHELLS), "seconds": time.perf_counter() - t0}
+    for name, b in bsums.items():
+        err = np.abs(b[sel] - exact)
+        rel = err / np.abs(exact)
+        out[name] = {"median_rel": float(np.median(rel)), "max_rel": float(rel.max()),
+                     "max_rel_cond_lt_1e3": float(rel[cond < 1e3].max()),
+                     "normalised_max": float((err / absum).max())}
+    return out
+
+
 def run_gpu(args, rank, world, local_rank):
     import torch
     import torch.distributed as dist
@@ -309,6 +358,7 @@ def run_gpu(args, rank, world, local_rank):
     torch.cuda.synchronize()
     b16, b32 = plans["bf16x3"].bsum.cpu().numpy(), plans["fp32"].bsum.cpu().numpy()
     rel = np.abs(b16 - b32) / np.abs(b32)
+    fp64 = None if args.no_fp64_check else fp64_error(half, plans)
 
     # end to end through the public API: pinned host positions in, host dict out
     import torch as _t
@@ -365,12 +415,48 @@ def run_gpu(args, rank, world, local_rank):
             "methods": results,
             "tc_over_fp32": results["fp32"]["ms_per_step"] / main["ms_per_step"],
             "tc_over_fp32_contraction": results["fp32"]["stage_ms"]["contraction"] / main["stage_ms"]["contraction"],
+            "fp64_error": fp64,
             "bf16x3_vs_fp32_rel": {"median": float(np.median(rel)), "p99": float(np.percentile(rel, 99)),
                                    "max": float(rel.max())},
             "roofline": roofline, "cpu_baseline": cpu,
             "e2e": {"value": world * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "api": "pyspectrum_gb300.pyspectrum.Bk_periodic(pinned xyz)"},
             "gpu_launches": main["gpu_launches"], "clocks": main["clocks"], "fft3d_comparator": fftcmp}
+    print(json.dumps(line), flush=True)
+
+
+def run_batch(args):
+    """Many boxes per call (Bk_periodic_batch): 64 seeded Zel'dovich mocks with
+    particle counts uniform in [0.5M, 4M] and grids mixed over {192, 256, 360}
+    (L = 2500, step 3, Nmax 40, split-BF16).  Prints one JSON line with the
+    batch time (positions already in pinned host memory; results back on the
+    host); not the headline bench line."""
+    import torch
+    from pyspectrum_gb300 import batch, mocks
+    rng = np.random.default_rng(4)
+    L = 2500.0
+    nmock = 64
+    grids = rng.choice([192, 256, 360], size=nmock)
+    nparts = rng.integers(500_000, 4_000_001, size=nmock)
+    cat = []
+    for k in range(nmock):
+        x = mocks.zeldovich_mock(int(nparts[k]), L, ngrid=int(grids[k]), seed=100 + k)
+        cat.append((torch.from_numpy(x.cpu().numpy()).pin_memory(), int(grids[k])))
+        del x
+    runner = batch.BkBatch(Lbox=L, step=3, Ncut=3, Nmax=40, method="bf16x3", graphs=True)
+    # first pass: plans, counts and graph capture for the three geometries
+    warm = [cat[int(np.nonzero(grids == g)[0][0])] for g in (192, 256, 360) for _ in range(2)]
+    runner.run(warm)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = runner.run(cat)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    assert len(out) == nmock and all(np.isfinite(o["b123"]).all() for o in out)
+    line = {"workload": "64 Zel'dovich mocks, Np in [0.5M, 4M], Ngrid in {192, 256, 360}, L 2500, step 3, Nmax 40",
+            "metric": "Bk evals/s (batch, host positions in, host results out)", "value": nmock / dt,
+            "seconds": dt, "mocks_per_grid": {str(g): int((grids == g).sum()) for g in (192, 256, 360)},
+            "particles_total": int(nparts.sum()), "method": "bf16x3", "graphs": True}
     print(json.dumps(line), flush=True)
 
 
@@ -410,12 +496,18 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-check", action="store_true", help="skip the float64 error check (about 30 s of CPU)")
     ap.add_argument("--small", action="store_true", help="run the 192^3 profiling case instead of the bench workload")
+    ap.add_argument("--batch", action="store_true",
+                    help="time 64 mixed-size mocks through Bk_periodic_batch instead of the bench workload")
     ap.add_argument("--profile-shells", type=int, default=0, metavar="J",
                     help="only run shells J-2..J of the bench workload three times (ncu profiling case)")
     args = ap.parse_args()
     if args.profile_shells:
         run_profile_shells(args.profile_shells)
+        return
+    if args.batch:
+        run_batch(args)
         return
     if args.small:
         WORKLOAD.clear()
