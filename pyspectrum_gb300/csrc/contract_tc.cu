@@ -5,23 +5,31 @@
 //   D[p, c] = sum_v P_p(v) F_c(v),   P_p = F_i F_j  (pair p = (i, j))
 // with pair rows on M (tiles of 128) and shells on N, the voxels on K.  Both
 // operands are split into bf16 hi + lo parts (x = hi + lo, lo = x - hi).  The
-// B operand holds the hi and lo rows of the shells interleaved in blocks of
-// 16 (rows [32b, 32b+16) = hi of shells [16b, 16b+16), the next 16 rows = lo),
-// so one MMA with N' = 2N gives A_x * B_hi and A_x * B_lo side by side; two
-// MMAs per k-step (A_hi, then A_lo, same B, same accumulator) produce all four
-// products (hi+lo)(hi+lo), which are summed over the hi/lo column pairs when
-// the accumulators are drained.  Small-N tcgen05.mma instructions are bound
-// by a per-instruction cost, so two wide MMAs beat three narrow ones.
+// B operand holds the hi and lo rows of the shells interleaved in blocks of 8
+// (rows [16b, 16b+8) = hi of shells [8b, 8b+8), the next 8 rows = lo).  A
+// tcgen05.mma costs about the same up to N = 128 whatever its N (measured:
+// ~86 cycles per instruction at N = 32..64), so the kernel issues as few as
+// TMEM allows:
+//   wide form: per tile and k-step two MMAs (A_hi, then A_lo) against all
+//     2N interleaved B rows, so the accumulator holds A_x B_hi and A_x B_lo
+//     side by side (all four products), summed when drained;
+//   narrow form (when 2N columns per tile do not fit): three MMAs (A_hi B_hi,
+//     A_lo B_hi, A_hi B_lo; A_lo B_lo, 2^-16 of the rest, is dropped) into
+//     N columns, B_hi and B_lo read through descriptors that skip the other
+//     part's 8-row blocks.
+// Consecutive MMAs go to the same accumulator (all of one tile's MMAs of a
+// chunk back to back): alternating accumulators issues slower.
 //
 // CTA layout (1 CTA per SM, persistent over a contiguous voxel range):
-//   warps 0-15 (512 threads): producers.  Warp w owns TMEM lane quarter w%4
-//     of pair tile w/4: lane l is pair row 128*(w/4) + 32*(w%4) + l.  Per
-//     chunk of KC = 32 voxels each thread forms its pair's 32 products,
-//     splits them into hi/lo bf16 and writes them straight into TMEM
-//     (tcgen05.st) as the MMA's A operand; threads < 4*nshell write the B
-//     operand (the shells' hi/lo parts) to shared memory in the UMMA K-major
-//     core-matrix layout.  Then `full[stage]` and `fempty[buffer]` are
-//     signalled (one arrival per warp).
+//   warps 0-15 (512 threads): producers, two groups of 8 warps on alternate
+//     chunks of KC = 32 voxels.  Warp w of a group owns TMEM lane quarter
+//     w % 4 of the tile pair (w % 8) / 4.  Each thread forms 4 voxels of 8
+//     pair rows (two runs of four rows that share their shells j), splits the
+//     products into hi/lo bf16 and writes them straight into TMEM
+//     (tcgen05.st, 16x256b shape) as the MMA's A operand; threads < 4*nshell
+//     write the B operand (the shells' hi and lo parts) to shared memory in
+//     the UMMA K-major core-matrix layout.  Then `full[stage]` and
+//     `fempty[buffer]` are signalled (one arrival per warp).
 //   warp 16, lane 0: issues tcgen05.mma (A from TMEM, B from shared memory)
 //     and tcgen05.commit to `empty[stage]`.
 //   warp 17, lane 0: streams the fields: one TMA tensor copy per chunk
@@ -32,7 +40,7 @@
 //   float32 sums per triangle in shared memory and arrive on `drained`; the
 //   next MMA restarts the accumulators.  At the end each CTA writes one float64
 //   partial per triangle; a second kernel adds the partials in a fixed order.
-// TMEM columns: [0, C) accumulators (2N per tile); then two A stages of 32
+// TMEM columns: [0, C) accumulators (2N or N per tile); then two A stages of 32
 // columns per tile.  Every mbarrier wait is bounded; on timeout the kernel
 // records an error code, stops issuing work, waits (bounded) for its copies
 // and MMAs in flight, frees its TMEM and returns.
@@ -52,7 +60,7 @@ namespace tc {
 constexpr int KC = 32;               // voxels per chunk (two k-steps of 16)
 constexpr int MAXROWS = 512;         // pair rows per CTA group (4 M-tiles)
 constexpr int MAXB = 64;             // shells
-constexpr int BROWS = 2 * MAXB;      // B operand rows (hi and lo of each shell)
+constexpr int BROWS = 2 * MAXB;      // B operand rows: hi and lo parts of shells 0..63
 constexpr int NSTAGE = 2;
 constexpr int NPROD = 512;           // producer threads (warps 0-15): 4 tiles x 4 TMEM lane quarters
 constexpr int PWARPS = NPROD / 32;
@@ -62,7 +70,7 @@ constexpr int NTHREADS = NPROD + 64; // + the MMA warp + the copy warp
 constexpr int SEG = 32;              // chunks between accumulator drains (TMEM float32 accumulation length sets the error: 128 chunks gave a bf16x3 median error of 8e-6 vs FP64, 64 gave 4e-6)
 constexpr int MAXGROUPS = 8;
 constexpr int MAXTILES = 4;
-constexpr int MAXCOLS = 256;         // accumulator columns per group (+ 2 x 4 x 32 A columns <= 512)
+constexpr int RT_PER_GROUP = 64;     // producer row threads per group: 2 tile pairs x 4 lane quarters x 8
 constexpr int ACOLS = 32;            // TMEM columns of one tile's A operand per stage (2 k-steps x (8 hi + 8 lo))
 constexpr int NFBUF = 6;             // field buffers in the copy ring
 constexpr unsigned long long kWaitNs = 2000000000ull;   // 2 s bound on any mbarrier wait
@@ -76,7 +84,8 @@ __host__ __device__ constexpr int fixed_smem(int nshell) { return 1024 + NFBUF *
 struct Group {
     int rows;              // pair rows used (<= 512)
     int ntiles;            // 128-row tiles
-    int tile_n[MAXTILES];  // N of each tile in shells (multiple of 16); the MMA uses 2N columns
+    int wide;              // 1: two MMAs per tile and k-step into 2N columns; 0: three into N
+    int tile_n[MAXTILES];  // N of each tile in shells (wide: multiple of 8; narrow: of 16; <= 64)
     int tile_col[MAXTILES];// TMEM column offset of each tile
     int ncols;             // TMEM columns allocated (power of 2 >= 32)
     int table_off;         // offset of this group in the row / slot tables
@@ -93,6 +102,9 @@ struct Params {
     // rows), lmin, lmax (the columns l of its triangles) and the first of its
     // Kahan slots; the row's columns l in [lmin, lmax] own consecutive slots
     const int16_t* pair_row;
+    // [group][64] per producer row thread: i0 | i1 << 8 | J0 << 16 | J1 << 24,
+    // its slots u = 0, 1: pair rows (i_u, J_u + y), y = 0..3
+    const int32_t* rt_tab;
     const int32_t* slot_tri;     // [group][maxslots] triangle index of each slot (-1: unused)
     double* partials;            // [gridDim.x][ntri]
     int* err;
@@ -159,10 +171,8 @@ __device__ __forceinline__ uint32_t make_idesc(int M, int N) {
 // core matrix (r/8, k/8) at (r/8)*512 + (k/8)*128, row r%8 at 16 B, element k%8 at 2 B.
 __device__ __forceinline__ int op_off(int r, int kgroup) { return (r >> 3) * 512 + kgroup * 128 + (r & 7) * 16; }
 
-// B operand row of shell s, part p (0 = hi, 1 = lo): hi/lo interleaved in blocks of 16
-__host__ __device__ __forceinline__ int brow(int s, int p) { return ((s >> 4) << 5) | (p << 4) | (s & 15); }
-// shell of accumulator column c (relative to its tile)
-__host__ __device__ __forceinline__ int col_shell(int c) { return ((c >> 5) << 4) | (c & 15); }
+// B operand row of shell s, part p (0 = hi, 1 = lo): hi/lo interleaved in blocks of 8
+__host__ __device__ __forceinline__ int brow(int s, int p) { return ((s >> 3) << 4) | (p << 3) | (s & 7); }
 
 // byte offset of the 16-byte chunk q (voxels 4q..4q+3) of field row r in a
 // buffer written by the TMA with 128-byte swizzle (chunk index XOR row % 8)
@@ -214,6 +224,80 @@ __device__ __forceinline__ void tmem_st8(uint32_t addr, const uint32_t* v) {
                  : "memory");
 }
 
+// tcgen05.st 16x256b.x4: 16 TMEM lanes x 32 columns, four repeats of 8
+// columns; in repeat k thread t writes (lane t/4, columns 8k + 2(t%4) + {0,1})
+// from v[4k], v[4k+1] and (lane t/4 + 8, same columns) from v[4k+2], v[4k+3]
+__device__ __forceinline__ void tmem_st16x256_x4(uint32_t addr, const uint32_t* v) {
+    asm volatile("tcgen05.st.sync.aligned.16x256b.x4.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
+                 :: "r"(addr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]),
+                    "r"(v[7]), "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]),
+                    "r"(v[15])
+                 : "memory");
+}
+
+// hi/lo bf16 parts of two floats (packed pairs)
+__device__ __forceinline__ void split2(float2 p, uint32_t& h, uint32_t& l) {
+    h = pack_bf16x2(p.x, p.y);
+    const float2 lv = sub2(p, make_float2(__uint_as_float(h << 16), __uint_as_float(h & 0xFFFF0000u)));
+    l = pack_bf16x2(lv.x, lv.y);
+}
+
+// One slot of a producer thread into TMEM: the products fi[ks] * fj[ks][y]
+// (4 voxels each, both k-steps) of its four pair rows y = 0..3, which sit at
+// lanes x + 8y of the lane quarter (`addr` = quarter base + the tile's A
+// columns of this stage).  Rows 0, 1 go to the 16-lane block [0, 16), rows
+// 2, 3 to [16, 32).  The 32 A columns of a stage are, per k-step, 8 hi then
+// 8 lo columns, so repeat k of the x4 shape is (k-step k/2, part k%2); lane
+// a of the thread group owns columns 2a, 2a + 1 of each repeat (voxels
+// 4a .. 4a + 3 of the k-step).
+__device__ __forceinline__ void store_slot(const float4* fi, const float4 (*fj)[4], uint32_t addr) {
+#pragma unroll
+    for (int blk = 0; blk < 2; ++blk) {
+        uint32_t v[16];
+#pragma unroll
+        for (int ks = 0; ks < 2; ++ks)
+#pragma unroll
+            for (int yy = 0; yy < 2; ++yy) {
+                const float4 f = fj[ks][2 * blk + yy];
+                const float4 g = fi[ks];
+                split2(mul2(make_float2(g.x, g.y), make_float2(f.x, f.y)), v[8 * ks + 2 * yy], v[8 * ks + 4 + 2 * yy]);
+                split2(mul2(make_float2(g.z, g.w), make_float2(f.z, f.w)), v[8 * ks + 2 * yy + 1],
+                       v[8 * ks + 4 + 2 * yy + 1]);
+            }
+        tmem_st16x256_x4(addr + ((uint32_t)(16 * blk) << 16), v);
+    }
+}
+
+// The MMAs of one chunk: per k-step and tile, A_hi then A_lo against the B
+// stage (wide form: all 2N interleaved rows), plus A_hi against B_lo (narrow
+// form: B_lo blocks 512 bytes after the B_hi blocks).  `first` == 0 starts
+// each accumulator afresh.
+template <bool WIDE, int NT>
+__device__ __forceinline__ void issue_chunk(const uint32_t (&dcol)[MAXTILES], const uint32_t (&aad)[NSTAGE][KC / 16][MAXTILES],
+                                            const uint64_t (&bdesc)[NSTAGE][KC / 16], const uint32_t (&idesc)[MAXTILES],
+                                            int s, uint32_t first) {
+#pragma unroll
+    for (int ks = 0; ks < KC / 16; ++ks) {
+        const uint32_t acc0 = ks == 0 ? first : 1u;
+        const uint64_t bd = s ? bdesc[1][ks] : bdesc[0][ks];
+#pragma unroll
+        for (int t = 0; t < NT; ++t) {
+            const uint32_t ahi = s ? aad[1][ks][t] : aad[0][ks][t];
+            asm volatile("{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n"
+                         :: "r"(dcol[t]), "r"(ahi), "l"(bd), "r"(idesc[t]), "r"(acc0));
+            asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, 1;"
+                         :: "r"(dcol[t]), "r"(ahi + 8u), "l"(bd), "r"(idesc[t]));
+            if constexpr (!WIDE)
+                asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, 1;"
+                             :: "r"(dcol[t]), "r"(ahi), "l"(bd + (uint64_t)(512 >> 4)), "r"(idesc[t]));
+        }
+    }
+}
+
+__device__ __forceinline__ float4 lds4(const unsigned char* base, uint32_t off) {
+    return *reinterpret_cast<const float4*>(base + off);
+}
+
 __global__ void __launch_bounds__(NTHREADS, 1)
 contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUtensorMap fmap) {
     extern __shared__ unsigned char smem_raw[];
@@ -242,7 +326,7 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
     const int nch = (int)max((int64_t)0, c1 - c0);
     __syncthreads();
     int C = 0;
-    for (int t = 0; t < G.ntiles; ++t) C = max(C, G.tile_col[t] + 2 * G.tile_n[t]);
+    for (int t = 0; t < G.ntiles; ++t) C = max(C, G.tile_col[t] + (G.wide ? 2 : 1) * G.tile_n[t]);
 
     // ---- set-up ----
     for (int i = tid; i < MAXROWS * 4; i += NTHREADS) pij[i] = P.pair_row[(size_t)G.table_off * 4 + i];
@@ -282,24 +366,35 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
         // ================= producers =================
         // Two groups of 8 warps take alternate chunks (group g: chunks c with
         // c % 2 == g, A / B stage g), so one group's shared-memory loads overlap
-        // the other's arithmetic.  Warp w of group g owns TMEM lane quarter w % 4
-        // of tiles (w % 8) / 4 and (w % 8) / 4 + 2: one pair row per tile.
+        // the other's arithmetic.  Warp w of a group owns TMEM lane quarter
+        // q = w % 4 of the tile pair p = (w % 8) / 4 (tiles 2p and 2p + 1).
+        // Lane 4x + a: x is one of the warp's 8 row threads, each with two
+        // slots; slot u lies in tile 2p + u and holds the pair rows
+        // (i_u, J_u + y), y = 0..3, at TMEM lanes 32q + x + 8y.  Lane a forms
+        // voxels 4a .. 4a+3 of every 16-voxel k-step of those 8 rows.  The
+        // plan gives both slots the same run J wherever it can, so a thread
+        // loads 6 field pieces per k-step for its 32 products.
         const int rows = G.rows;
         const int nsh = P.nshell;
         const int grp = warp >> 3;
         const int gtid = tid & 255;                   // thread index within the group
-        int ri[2], rj[2];
-        bool ton[2], ron[2];
+        const int tp = (warp & 7) >> 2;
+        const bool tp_on = 2 * tp < G.ntiles;         // warp-uniform
+        const int ax = lane & 3;
+        const uint32_t code =
+            (uint32_t)P.rt_tab[(size_t)blockIdx.y * RT_PER_GROUP + tp * 32 + q * 8 + (lane >> 2)];
+        // byte offset of this lane's 16-byte piece of field row r in k-step 0
+        // (k-step 1: XOR 64, the other half of the 128-byte swizzled row)
+        auto foff = [&](int r) {
+            r = min(r, nsh - 1);
+            return (uint32_t)(r * 128 + ((ax ^ (r & 7)) << 4));
+        };
+        const uint32_t oi0 = foff((int)(code & 0xffu)), oi1 = foff((int)((code >> 8) & 0xffu));
+        const int J0 = (int)((code >> 16) & 0xffu), J1 = (int)(code >> 24);
+        const bool reload = J1 != J0;
+        uint32_t oj0[4];
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            const int t = ((warp & 7) >> 2) + 2 * u;  // warp-uniform
-            const int row = 128 * t + 32 * q + lane;
-            ton[u] = t < G.ntiles;
-            ron[u] = ton[u] && row < rows && pij[4 * row] >= 0;
-            ri[u] = ron[u] ? (pij[4 * row] & 0xff) : 0;
-            rj[u] = ron[u] ? (pij[4 * row] >> 8) : 0;
-        }
-        const int tl[2] = {(warp & 7) >> 2, ((warp & 7) >> 2) + 2};
+        for (int y = 0; y < 4; ++y) oj0[y] = foff(J0 + y);
         // B writer: shell r, k-group g (voxels 8g..8g+7); 4 nshell <= 256 threads per group
         int ub_r = -1, ub_g = 0;
         if (gtid < nsh * 4) {
@@ -313,30 +408,28 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
         auto drain = [&]() -> bool {
             if (!warp_wait(smem_u32(&bar_seg), seg_count & 1)) return false;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            // the four warps of this lane quarter take 32-column groups
-            // (hi and lo columns of 16 shells) round-robin; one thread adds
-            // the hi and lo parts of a (row, shell) and updates its slot
-            for (int cg = 32 * ((warp >> 2) & 3); cg < C; cg += 128) {
-                uint32_t d[32];
+            // the four warps of this lane quarter take 16-column groups
+            // round-robin (wide form: the hi and lo columns of 8 shells;
+            // narrow: 16 shells); one thread adds a (row, shell) into its slot
+            const bool wide = G.wide != 0;
+            for (int cg = 16 * ((warp >> 2) & 3); cg < C; cg += 64) {
+                uint32_t d[16];
                 tmem_ld8(lane_base + (uint32_t)cg, d);
                 tmem_ld8(lane_base + (uint32_t)cg + 8u, d + 8);
-                tmem_ld8(lane_base + (uint32_t)cg + 16u, d + 16);
-                tmem_ld8(lane_base + (uint32_t)cg + 24u, d + 24);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                 int t = 0;
                 while (t + 1 < G.ntiles && cg >= G.tile_col[t + 1]) ++t;
-                if (cg >= G.tile_col[t] + 2 * G.tile_n[t]) continue;
                 const int drow = 128 * t + 32 * q + lane;
                 // this row's columns l in [lmin, lmax] own slots base + (l - lmin)
                 const short4 pr = drow < rows ? *reinterpret_cast<const short4*>(&pij[4 * drow])
                                               : make_short4(-1, 0, -1, 0);
-                const int sh0 = col_shell(cg - G.tile_col[t]);
+                const int sh0 = wide ? (cg - G.tile_col[t]) >> 1 : cg - G.tile_col[t];
 #pragma unroll
                 for (int e = 0; e < 16; ++e) {
                     const int l = sh0 + e;
-                    if (pr.x < 0 || l < pr.y || l > pr.z) continue;
+                    if ((wide && e >= 8) || pr.x < 0 || l < pr.y || l > pr.z) continue;
                     const int slot = pr.w + (l - pr.y);
-                    const float v = __uint_as_float(d[e]) + __uint_as_float(d[16 + e]);
+                    const float v = wide ? __uint_as_float(d[e]) + __uint_as_float(d[e + 8]) : __uint_as_float(d[e]);
                     const float2 a = acc[slot];
                     const float y = v - a.y;
                     const float sum = a.x + y;
@@ -383,34 +476,26 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
                                      make_float2(e.z, e.w)};
                 split_store8(x, Bst + op_off(brow(ub_r, 0), ub_g), Bst + op_off(brow(ub_r, 1), ub_g));
             }
-            // A operand: this lane's pair products of both tiles, straight into TMEM
-#pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                if (!ton[u]) continue;                // warp-uniform
+            // A operand: this thread's 8 pair rows x 4 voxels per k-step, straight into TMEM
+            if (tp_on) {
+                float4 fi0[2], fi1[2], fj[2][4];
 #pragma unroll
                 for (int ks = 0; ks < KC / 16; ++ks) {
-                    uint32_t h[8], l[8];
+                    const uint32_t kx = ks ? 64u : 0u;
+                    fi0[ks] = lds4(F, oi0 ^ kx);
 #pragma unroll
-                    for (int g = 0; g < 4; ++g) {
-                        float4 a = make_float4(0.f, 0.f, 0.f, 0.f), e = a;
-                        if (ron[u]) {
-                            a = *reinterpret_cast<const float4*>(F + fchunk(ri[u], 4 * ks + g));
-                            e = *reinterpret_cast<const float4*>(F + fchunk(rj[u], 4 * ks + g));
-                        }
-                        const float2 p0 = mul2(make_float2(a.x, a.y), make_float2(e.x, e.y));
-                        const float2 p1 = mul2(make_float2(a.z, a.w), make_float2(e.z, e.w));
-                        h[2 * g] = pack_bf16x2(p0.x, p0.y);
-                        h[2 * g + 1] = pack_bf16x2(p1.x, p1.y);
-                        const float2 l0 = sub2(p0, make_float2(__uint_as_float(h[2 * g] << 16),
-                                                               __uint_as_float(h[2 * g] & 0xFFFF0000u)));
-                        const float2 l1 = sub2(p1, make_float2(__uint_as_float(h[2 * g + 1] << 16),
-                                                               __uint_as_float(h[2 * g + 1] & 0xFFFF0000u)));
-                        l[2 * g] = pack_bf16x2(l0.x, l0.y);
-                        l[2 * g + 1] = pack_bf16x2(l1.x, l1.y);
-                    }
-                    tmem_st8(lane_base + acol(s, tl[u], ks), h);
-                    tmem_st8(lane_base + acol(s, tl[u], ks) + 8u, l);
+                    for (int y = 0; y < 4; ++y) fj[ks][y] = lds4(F, oj0[y] ^ kx);
                 }
+                store_slot(fi0, fj, lane_base + acol(s, 2 * tp, 0));
+                fi1[0] = lds4(F, oi1);
+                fi1[1] = lds4(F, oi1 ^ 64u);
+                if (reload) {
+#pragma unroll
+                    for (int ks = 0; ks < KC / 16; ++ks)
+#pragma unroll
+                        for (int y = 0; y < 4; ++y) fj[ks][y] = lds4(F, foff(J1 + y) ^ (ks ? 64u : 0u));
+                }
+                store_slot(fi1, fj, lane_base + acol(s, 2 * tp + 1, 0));
             }
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -433,43 +518,42 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
             // Every operand address is computed once: B descriptors per
             // (stage, k-step), A TMEM addresses per (stage, k-step, tile).
             const int ntiles = G.ntiles;
+            const bool wide = G.wide != 0;
             uint32_t idesc[MAXTILES], dcol[MAXTILES];
 #pragma unroll
             for (int t = 0; t < MAXTILES; ++t) {
-                idesc[t] = make_idesc(128, 2 * G.tile_n[t]);
+                idesc[t] = make_idesc(128, (wide ? 2 : 1) * G.tile_n[t]);
                 dcol[t] = tmem + (uint32_t)G.tile_col[t];
             }
             const uint32_t sbase = smem_u32(stage_base);
+            // B descriptors: wide form all rows (8-row blocks 512 bytes
+            // apart); narrow form the hi blocks only (1024 apart; the lo
+            // blocks are 512 bytes further)
             uint64_t bdesc[NSTAGE][KC / 16];
             uint32_t aad[NSTAGE][KC / 16][MAXTILES];
 #pragma unroll
             for (int s = 0; s < NSTAGE; ++s)
 #pragma unroll
                 for (int ks = 0; ks < KC / 16; ++ks) {
-                    bdesc[s][ks] = make_desc(sbase + (uint32_t)(s * STAGE_BYTES) + (uint32_t)(ks * 256), 128, 512);
+                    bdesc[s][ks] = make_desc(sbase + (uint32_t)(s * STAGE_BYTES) + (uint32_t)(ks * 256), 128,
+                                             wide ? 512 : 1024);
 #pragma unroll
                     for (int t = 0; t < MAXTILES; ++t) aad[s][ks][t] = tmem + acol(s, t, ks);
                 }
+            const int mode = (wide ? 2 : 0) + (ntiles > 2 ? 1 : 0);
             int seg_count = 0;
             uint32_t first = 0;   // 0: the next MMA of each tile overwrites its accumulator
             for (int c = 0; c < nch; ++c) {
                 const int s = c & 1;
                 if (!mbar_wait(smem_u32(&bar_full[s]), (c >> 1) & 1)) { atomicExch(P.err, 3); abort_flag = 1; break; }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-                for (int ks = 0; ks < KC / 16; ++ks) {
-                    const uint64_t bd = s ? bdesc[1][ks] : bdesc[0][ks];
-                    const uint32_t acc0 = ks == 0 ? first : 1u;
-#pragma unroll
-                    for (int t = 0; t < MAXTILES; ++t) {
-                        if (t < ntiles) {
-                            const uint32_t ahi = s ? aad[1][ks][t] : aad[0][ks][t];
-                            asm volatile("{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n"
-                                         :: "r"(dcol[t]), "r"(ahi), "l"(bd), "r"(idesc[t]), "r"(acc0));
-                            asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, 1;"
-                                         :: "r"(dcol[t]), "r"(ahi + 8u), "l"(bd), "r"(idesc[t]));
-                        }
-                    }
+                // one branch-free MMA sequence per (form, tile count): a
+                // branch between the MMAs of a chunk slows their issue by ~30 %
+                switch (mode) {
+                    case 0: issue_chunk<false, 2>(dcol, aad, bdesc, idesc, s, first); break;
+                    case 1: issue_chunk<false, 4>(dcol, aad, bdesc, idesc, s, first); break;
+                    case 2: issue_chunk<true, 2>(dcol, aad, bdesc, idesc, s, first); break;
+                    default: issue_chunk<true, 4>(dcol, aad, bdesc, idesc, s, first); break;
                 }
                 first = 1u;
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
@@ -533,16 +617,23 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
 }
 
 // ---------------------------------------------------------------------------
-// host planning: pairs (i, j) = the two largest shell slots of each triangle,
-// column = the smallest.  Pairs sorted by (j, i) keep each tile's columns
-// short.  Plans are cached per triangle list.
+// host planning.  Pairs (i, j) = the two largest shell slots of each
+// triangle, column = the smallest.  The pairs of each shell i are cut into
+// runs of four consecutive shells j (a "slot": rows (i, J + y), y = 0..3, some
+// of them padding); two slots with the same run J make one producer row
+// thread (its loads of F_J .. F_J+3 serve both).  Row threads are sorted by
+// J so each tile's columns stay short, and the two threads that share a
+// quarter-warp load phase are matched to keep their shared-memory reads in
+// different banks.  Plans are cached per triangle list.
 // ---------------------------------------------------------------------------
 struct HostPlan {
     Params base;           // pointers filled at launch
     std::vector<int16_t> pair_row;
+    std::vector<int32_t> rt_tab;
     std::vector<int32_t> slot_tri;
-    std::vector<char> image;      // pair_row | slot_tri, each 256-byte aligned (device layout)
+    std::vector<char> image;      // pair_row | rt_tab | slot_tri, each 256-byte aligned (device layout)
     const void* image_src = nullptr;   // page-locked copy of `image` (or image.data())
+    size_t off_rt = 0;
     size_t off_stri = 0;
     size_t smem = 0;
     bool ok = false;
@@ -558,6 +649,25 @@ static std::map<std::vector<int32_t>, HostPlan*> g_plans;
 static int pow2_cols(int n) {
     int c = 32;
     while (c < n) c <<= 1;
+    return c;
+}
+
+struct PlanSlot {
+    int i, J, mask;   // rows (i, J + y) for the set bits y of mask
+};
+struct RowThread {
+    PlanSlot s[2];
+};
+
+// Extra shared-memory wavefronts when two row threads share a load phase:
+// two different field rows conflict when their 16-byte pieces fall in the
+// same half of the 128-byte swizzled row (bit 2 of the row index equal).
+static int phase_conflicts(const RowThread& A, const RowThread& B) {
+    auto clash = [](int r, int t) { return r != t && ((r >> 2) & 1) == ((t >> 2) & 1); };
+    int c = clash(A.s[0].i, B.s[0].i) + clash(A.s[1].i, B.s[1].i);
+    for (int y = 0; y < 4; ++y) c += clash(A.s[0].J + y, B.s[0].J + y);
+    if (A.s[1].J != A.s[0].J || B.s[1].J != B.s[0].J)
+        for (int y = 0; y < 4; ++y) c += clash(A.s[1].J + y, B.s[1].J + y);
     return c;
 }
 
@@ -584,56 +694,69 @@ static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri) {
             return hp;
         }
     }
-    std::vector<std::pair<int, int>> order;
-    for (auto& kv : pairs) order.push_back(kv.first);
-    std::sort(order.begin(), order.end(), [](const std::pair<int, int>& x, const std::pair<int, int>& y) {
-        return x.second != y.second ? x.second < y.second : x.first < y.first;
-    });
-    const int nrows = (int)order.size();
-    // each row owns the Kahan slots of columns [lmin, lmax] of its triangles
-    auto row_slots = [&](const std::pair<int, int>& key) {
-        const auto& m = pairs[key];
-        return m.rbegin()->first - m.begin()->first + 1;
-    };
-    // N of each 128-row tile: the largest shell column it needs, rounded to 16;
-    // and the number of Kahan slots it holds
-    std::vector<int> tile_n, tile_slots;
-    for (int r0 = 0; r0 < nrows; r0 += 128) {
-        int maxl = 0, ns = 0;
-        for (int r = r0; r < std::min(nrows, r0 + 128); ++r) {
-            maxl = std::max(maxl, pairs[order[r]].rbegin()->first);
-            ns += row_slots(order[r]);
+    // slots: runs of four shells j per pair shell i
+    std::map<int, std::vector<int>> byi;
+    for (auto& kv : pairs) byi[kv.first.first].push_back(kv.first.second);
+    std::map<int, std::vector<PlanSlot>> byJ;
+    for (auto& kv : byi) {
+        std::vector<int>& js = kv.second;
+        std::sort(js.begin(), js.end());
+        for (size_t k = 0; k < js.size();) {
+            PlanSlot sl{kv.first, js[k], 0};
+            while (k < js.size() && js[k] <= sl.J + 3) sl.mask |= 1 << (js[k++] - sl.J);
+            byJ[sl.J].push_back(sl);
         }
-        tile_n.push_back(((maxl + 1) + 15) / 16 * 16);
-        tile_slots.push_back(ns);
     }
-    const int ntiles_all = (int)tile_n.size();
+    // row threads: two slots of the same run; the rest paired in run order
+    std::vector<RowThread> rts;
+    std::vector<PlanSlot> single;
+    for (auto& kv : byJ) {
+        const std::vector<PlanSlot>& v = kv.second;
+        size_t k = 0;
+        for (; k + 1 < v.size(); k += 2) rts.push_back(RowThread{{v[k], v[k + 1]}});
+        if (k < v.size()) single.push_back(v[k]);
+    }
+    for (size_t k = 0; k < single.size(); k += 2) {
+        const PlanSlot other = k + 1 < single.size() ? single[k + 1] : PlanSlot{single[k].i, single[k].J, 0};
+        rts.push_back(RowThread{{single[k], other}});
+    }
+    std::stable_sort(rts.begin(), rts.end(), [](const RowThread& x, const RowThread& y) {
+        const int jx = std::max(x.s[0].J, x.s[1].J), jy = std::max(y.s[0].J, y.s[1].J);
+        return jx != jy ? jx < jy : x.s[0].i < y.s[0].i;
+    });
+    auto rt_slots = [&](const RowThread& r) {
+        int n = 0;
+        for (int u = 0; u < 2; ++u)
+            for (int y = 0; y < 4; ++y)
+                if (r.s[u].mask >> y & 1) {
+                    const auto& m = pairs[{r.s[u].i, r.s[u].J + y}];
+                    n += m.rbegin()->first - m.begin()->first + 1;
+                }
+        return n;
+    };
     const size_t fixed = (size_t)fixed_smem(nshell);
     const int budget = (int)((227 * 1024 - 8192 - fixed) / sizeof(float2));
-    // Greedy grouping into CTA groups: at most 4 tiles, MAXCOLS accumulator
-    // columns (2N per tile; TMEM also holds 2 stages x 4 tiles x 32 A columns)
-    // and `budget` Kahan slots in shared memory.
-    std::vector<int> group_first;
+    // CTA groups: up to 64 consecutive row threads and `budget` Kahan slots
+    std::vector<size_t> group_first;
     {
-        int cur_tiles = 0, cur_cols = 0, cur_slots = 0;
-        for (int t = 0; t < ntiles_all; ++t) {
-            if (tile_slots[t] > budget) {
-                snprintf(hp->why, sizeof(hp->why), "a 128-row tile holds %d triangles (limit %d)", tile_slots[t], budget);
+        int cur = 0, cur_slots = 0;
+        for (size_t k = 0; k < rts.size(); ++k) {
+            const int ns = rt_slots(rts[k]);
+            if (ns > budget) {
+                snprintf(hp->why, sizeof(hp->why), "a row thread holds %d triangles (limit %d)", ns, budget);
                 return hp;
             }
-            if (cur_tiles == 0 || cur_tiles == MAXTILES || cur_cols + 2 * tile_n[t] > MAXCOLS ||
-                cur_slots + tile_slots[t] > budget) {
-                group_first.push_back(t);
-                cur_tiles = cur_cols = cur_slots = 0;
+            if (k == 0 || cur == RT_PER_GROUP || cur_slots + ns > budget) {
+                group_first.push_back(k);
+                cur = cur_slots = 0;
             }
-            ++cur_tiles;
-            cur_cols += 2 * tile_n[t];
-            cur_slots += tile_slots[t];
+            ++cur;
+            cur_slots += ns;
         }
     }
     const int ngroups = (int)group_first.size();
     if (ngroups > MAXGROUPS || ngroups == 0) {
-        snprintf(hp->why, sizeof(hp->why), "too many pair rows (%d) for the BF16x3 contraction", nrows);
+        snprintf(hp->why, sizeof(hp->why), "too many pair rows (%zu) for the BF16x3 contraction", pairs.size());
         return hp;
     }
     P.ngroups = ngroups;
@@ -641,45 +764,78 @@ static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri) {
     P.ntri = ntri;
     hp->pair_row.assign((size_t)ngroups * MAXROWS * 4, (int16_t)0);
     for (size_t r = 0; r < (size_t)ngroups * MAXROWS; ++r) hp->pair_row[4 * r] = -1;
+    hp->rt_tab.assign((size_t)ngroups * RT_PER_GROUP, 0);
     std::vector<std::vector<int32_t>> gslots(ngroups);
     int maxslots = 1;
     for (int g = 0; g < ngroups; ++g) {
         Group& G = P.g[g];
-        const int t0 = group_first[g];
-        const int t1 = g + 1 < ngroups ? group_first[g + 1] : ntiles_all;
-        const int r0 = 128 * t0;
-        G.rows = std::min(128 * (t1 - t0), nrows - r0);
-        G.ntiles = t1 - t0;
+        const size_t k0 = group_first[g];
+        const size_t k1 = g + 1 < ngroups ? group_first[g + 1] : rts.size();
+        const int n = (int)(k1 - k0);
+        G.ntiles = n > RT_PER_GROUP / 2 ? 4 : 2;
+        G.rows = 128 * G.ntiles;
         G.table_off = g * MAXROWS;
+        int tile_maxl[MAXTILES] = {0, 0, 0, 0};
+        for (int tp = 0; tp * 32 < n; ++tp) {
+            // match the 32 row threads of this tile pair into load-phase partners
+            std::vector<RowThread> blk(rts.begin() + k0 + 32 * tp, rts.begin() + k0 + std::min(n, 32 * (tp + 1)));
+            std::vector<int> order;
+            std::vector<bool> used(blk.size(), false);
+            for (size_t x = 0; x < blk.size(); ++x) {
+                if (used[x]) continue;
+                used[x] = true;
+                order.push_back((int)x);
+                int best = -1, bc = 0;
+                for (size_t y = x + 1; y < blk.size(); ++y) {
+                    if (used[y]) continue;
+                    const int c = phase_conflicts(blk[x], blk[y]);
+                    if (best < 0 || c < bc) { best = (int)y; bc = c; }
+                }
+                if (best >= 0) { used[best] = true; order.push_back(best); }
+            }
+            for (size_t pos = 0; pos < order.size(); ++pos) {
+                const RowThread& r = blk[order[pos]];
+                const int q = (int)pos / 8, x = (int)pos % 8;
+                hp->rt_tab[(size_t)g * RT_PER_GROUP + 32 * tp + pos] =
+                    (int32_t)((uint32_t)r.s[0].i | (uint32_t)r.s[1].i << 8 | (uint32_t)r.s[0].J << 16 |
+                              (uint32_t)r.s[1].J << 24);
+                for (int u = 0; u < 2; ++u) {
+                    const int tile = 2 * tp + u;
+                    for (int y = 0; y < 4; ++y) {
+                        if (!(r.s[u].mask >> y & 1)) continue;
+                        const int i = r.s[u].i, j = r.s[u].J + y;
+                        const auto& m = pairs[{i, j}];
+                        const int lmin = m.begin()->first, lmax = m.rbegin()->first;
+                        const int row = 128 * tile + 32 * q + x + 8 * y;
+                        int16_t* pr = &hp->pair_row[((size_t)G.table_off + row) * 4];
+                        pr[0] = (int16_t)(i | (j << 8));
+                        pr[1] = (int16_t)lmin;
+                        pr[2] = (int16_t)lmax;
+                        pr[3] = (int16_t)gslots[g].size();
+                        for (int l = lmin; l <= lmax; ++l) {
+                            auto it = m.find(l);
+                            gslots[g].push_back(it == m.end() ? -1 : it->second);
+                        }
+                        tile_maxl[tile] = std::max(tile_maxl[tile], lmax);
+                    }
+                }
+            }
+        }
+        // wide form when the 2N columns of all tiles fit beside the A stages
+        int wide_cols = 0;
+        for (int t = 0; t < G.ntiles; ++t) wide_cols += 2 * ((tile_maxl[t] + 1 + 7) / 8 * 8);
+        G.wide = wide_cols <= 512 - NSTAGE * MAXTILES * ACOLS ? 1 : 0;
         int col = 0;
         for (int t = 0; t < MAXTILES; ++t) { G.tile_n[t] = 16; G.tile_col[t] = 0; }
         for (int t = 0; t < G.ntiles; ++t) {
-            G.tile_n[t] = tile_n[t0 + t];
+            G.tile_n[t] = G.wide ? (tile_maxl[t] + 1 + 7) / 8 * 8 : (tile_maxl[t] + 1 + 15) / 16 * 16;
             G.tile_col[t] = col;
-            col += 2 * G.tile_n[t];
-            if (G.tile_n[t] > MAXB) {
-                snprintf(hp->why, sizeof(hp->why), "BF16x3 contraction supports at most %d shells", MAXB);
-                return hp;
-            }
+            col += (G.wide ? 2 : 1) * G.tile_n[t];
         }
         G.ncols = pow2_cols(col + NSTAGE * MAXTILES * ACOLS);
         if (G.ncols > 512) {
             snprintf(hp->why, sizeof(hp->why), "BF16x3 tile columns exceed TMEM");
             return hp;
-        }
-        for (int r = 0; r < G.rows; ++r) {
-            auto key = order[r0 + r];
-            const auto& m = pairs[key];
-            const int lmin = m.begin()->first, lmax = m.rbegin()->first;
-            int16_t* pr = &hp->pair_row[((size_t)G.table_off + r) * 4];
-            pr[0] = (int16_t)(key.first | (key.second << 8));
-            pr[1] = (int16_t)lmin;
-            pr[2] = (int16_t)lmax;
-            pr[3] = (int16_t)gslots[g].size();
-            for (int l = lmin; l <= lmax; ++l) {
-                auto it = m.find(l);
-                gslots[g].push_back(it == m.end() ? -1 : it->second);
-            }
         }
         G.nslots = (int)gslots[g].size();
         if (G.nslots > 32767) {
@@ -693,9 +849,11 @@ static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri) {
     for (int g = 0; g < ngroups; ++g)
         for (size_t i = 0; i < gslots[g].size(); ++i) hp->slot_tri[(size_t)g * maxslots + i] = gslots[g][i];
     hp->smem = fixed + sizeof(float2) * (size_t)maxslots;
-    hp->off_stri = al256(hp->pair_row.size() * 2);
+    hp->off_rt = al256(hp->pair_row.size() * 2);
+    hp->off_stri = hp->off_rt + al256(hp->rt_tab.size() * 4);
     hp->image.assign(hp->off_stri + al256(hp->slot_tri.size() * 4), 0);
     memcpy(hp->image.data(), hp->pair_row.data(), hp->pair_row.size() * 2);
+    memcpy(hp->image.data() + hp->off_rt, hp->rt_tab.data(), hp->rt_tab.size() * 4);
     memcpy(hp->image.data() + hp->off_stri, hp->slot_tri.data(), hp->slot_tri.size() * 4);
     hp->image_src = pinned_copy(hp->image.data(), hp->image.size());
     if (hp->image_src == nullptr) hp->image_src = hp->image.data();
@@ -730,7 +888,8 @@ size_t contract_tc_ws(int64_t nvox, int nshell, int ntri) {
     // + one gap slot per row and shell) + partials + error word
     (void)nshell;
     const size_t rows = (size_t)tc::MAXGROUPS * tc::MAXROWS;
-    const size_t tables = rows * 4 * 2 + (size_t)tc::MAXGROUPS * ((size_t)ntri + tc::MAXROWS * tc::MAXB) * 4 + 4096;
+    const size_t tables = rows * 4 * 2 + (size_t)tc::MAXGROUPS * tc::RT_PER_GROUP * 4 +
+                          (size_t)tc::MAXGROUPS * ((size_t)ntri + tc::MAXROWS * tc::MAXB) * 4 + 4096;
     const int64_t nchunks = (nvox + tc::KC - 1) / tc::KC;
     const size_t gx = (size_t)std::min<int64_t>(std::max<int64_t>(nchunks, 1), 1024);
     return tc::al256(tables) + tc::al256(gx * (size_t)std::max(ntri, 1) * sizeof(double)) + 256;
@@ -797,6 +956,7 @@ int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_
     int* d_err = reinterpret_cast<int*>(w + off); off += 256;      // status word first
     char* d_image = w + off;
     const int16_t* d_rows = reinterpret_cast<const int16_t*>(d_image);
+    const int32_t* d_rt = reinterpret_cast<const int32_t*>(d_image + hp->off_rt);
     const int32_t* d_stri = reinterpret_cast<const int32_t*>(d_image + hp->off_stri);
     off += hp->image.size();
     off = al256(off);
@@ -815,6 +975,7 @@ int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_
     P.nchunks = nchunks;
     P.chunks_per_cta = (nchunks + gx - 1) / gx;
     P.pair_row = d_rows;
+    P.rt_tab = d_rt;
     P.slot_tri = d_stri;
     P.partials = partials;
     P.err = d_err;
