@@ -62,7 +62,7 @@ constexpr int MAXROWS = 512;         // pair rows per CTA group (4 M-tiles)
 constexpr int MAXB = 64;             // shells
 constexpr int BROWS = 2 * MAXB;      // B operand rows: hi and lo parts of shells 0..63
 constexpr int NSTAGE = 2;
-constexpr int NPROD = 512;           // producer threads (warps 0-15): 4 tiles x 4 TMEM lane quarters
+constexpr int NPROD = 512;           // producer threads (warps 0-15): 2 k-steps x 2 tile pairs x 4 lane quarters
 constexpr int PWARPS = NPROD / 32;
 constexpr int MMA_WARP = PWARPS;
 constexpr int TMA_WARP = PWARPS + 1;
@@ -224,14 +224,14 @@ __device__ __forceinline__ void tmem_st8(uint32_t addr, const uint32_t* v) {
                  : "memory");
 }
 
-// tcgen05.st 16x256b.x4: 16 TMEM lanes x 32 columns, four repeats of 8
+// tcgen05.st 16x256b.x2: 16 TMEM lanes x 16 columns, two repeats of 8
 // columns; in repeat k thread t writes (lane t/4, columns 8k + 2(t%4) + {0,1})
 // from v[4k], v[4k+1] and (lane t/4 + 8, same columns) from v[4k+2], v[4k+3]
-__device__ __forceinline__ void tmem_st16x256_x4(uint32_t addr, const uint32_t* v) {
-    asm volatile("tcgen05.st.sync.aligned.16x256b.x4.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
+// (layout checked on the GPU for the x1 and x4 forms of the shape)
+__device__ __forceinline__ void tmem_st16x256_x2(uint32_t addr, const uint32_t* v) {
+    asm volatile("tcgen05.st.sync.aligned.16x256b.x2.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};"
                  :: "r"(addr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]),
-                    "r"(v[7]), "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]),
-                    "r"(v[15])
+                    "r"(v[7])
                  : "memory");
 }
 
@@ -242,47 +242,43 @@ __device__ __forceinline__ void split2(float2 p, uint32_t& h, uint32_t& l) {
     l = pack_bf16x2(lv.x, lv.y);
 }
 
-// One slot of a producer thread into TMEM: the products fi[ks] * fj[ks][y]
-// (4 voxels each, both k-steps) of its four pair rows y = 0..3, which sit at
+// One slot of a producer thread into TMEM for its k-step: the products
+// fi * fj[y] (4 voxels each) of its four pair rows y = 0..3, which sit at
 // lanes x + 8y of the lane quarter (`addr` = quarter base + the tile's A
-// columns of this stage).  Rows 0, 1 go to the 16-lane block [0, 16), rows
-// 2, 3 to [16, 32).  The 32 A columns of a stage are, per k-step, 8 hi then
-// 8 lo columns, so repeat k of the x4 shape is (k-step k/2, part k%2); lane
-// a of the thread group owns columns 2a, 2a + 1 of each repeat (voxels
-// 4a .. 4a + 3 of the k-step).
-__device__ __forceinline__ void store_slot(const float4* fi, const float4 (*fj)[4], uint32_t addr) {
+// columns of this stage and k-step: 8 hi then 8 lo columns).  Rows 0, 1 go
+// to the 16-lane block [0, 16), rows 2, 3 to [16, 32); repeat 0 of the x2
+// shape carries the hi parts, repeat 1 the lo parts; lane a of the thread
+// group owns columns 2a, 2a + 1 of each repeat (voxels 4a .. 4a + 3).
+__device__ __forceinline__ void store_slot(float4 fi, const float4* fj, uint32_t addr) {
 #pragma unroll
     for (int blk = 0; blk < 2; ++blk) {
-        uint32_t v[16];
+        uint32_t v[8];
 #pragma unroll
-        for (int ks = 0; ks < 2; ++ks)
-#pragma unroll
-            for (int yy = 0; yy < 2; ++yy) {
-                const float4 f = fj[ks][2 * blk + yy];
-                const float4 g = fi[ks];
-                split2(mul2(make_float2(g.x, g.y), make_float2(f.x, f.y)), v[8 * ks + 2 * yy], v[8 * ks + 4 + 2 * yy]);
-                split2(mul2(make_float2(g.z, g.w), make_float2(f.z, f.w)), v[8 * ks + 2 * yy + 1],
-                       v[8 * ks + 4 + 2 * yy + 1]);
-            }
-        tmem_st16x256_x4(addr + ((uint32_t)(16 * blk) << 16), v);
+        for (int yy = 0; yy < 2; ++yy) {
+            const float4 f = fj[2 * blk + yy];
+            split2(mul2(make_float2(fi.x, fi.y), make_float2(f.x, f.y)), v[2 * yy], v[4 + 2 * yy]);
+            split2(mul2(make_float2(fi.z, fi.w), make_float2(f.z, f.w)), v[2 * yy + 1], v[4 + 2 * yy + 1]);
+        }
+        tmem_st16x256_x2(addr + ((uint32_t)(16 * blk) << 16), v);
     }
 }
 
 // The MMAs of one chunk: per k-step and tile, A_hi then A_lo against the B
 // stage (wide form: all 2N interleaved rows), plus A_hi against B_lo (narrow
-// form: B_lo blocks 512 bytes after the B_hi blocks).  `first` == 0 starts
-// each accumulator afresh.
+// form: B_lo blocks 512 bytes after the B_hi blocks).  `abase` = TMEM address
+// of the stage's A columns (tile t, k-step ks at + 32 t + 16 ks), `bd0` = the
+// stage's B descriptor (k-step ks at + 256 bytes).  `first` == 0 starts each
+// accumulator afresh.
 template <bool WIDE, int NT>
-__device__ __forceinline__ void issue_chunk(const uint32_t (&dcol)[MAXTILES], const uint32_t (&aad)[NSTAGE][KC / 16][MAXTILES],
-                                            const uint64_t (&bdesc)[NSTAGE][KC / 16], const uint32_t (&idesc)[MAXTILES],
-                                            int s, uint32_t first) {
+__device__ __forceinline__ void issue_chunk(const uint32_t (&dcol)[MAXTILES], uint32_t abase, uint64_t bd0,
+                                            const uint32_t (&idesc)[MAXTILES], uint32_t first) {
 #pragma unroll
     for (int ks = 0; ks < KC / 16; ++ks) {
         const uint32_t acc0 = ks == 0 ? first : 1u;
-        const uint64_t bd = s ? bdesc[1][ks] : bdesc[0][ks];
+        const uint64_t bd = bd0 + (uint64_t)((ks * 256) >> 4);
 #pragma unroll
         for (int t = 0; t < NT; ++t) {
-            const uint32_t ahi = s ? aad[1][ks][t] : aad[0][ks][t];
+            const uint32_t ahi = abase + (uint32_t)(t * ACOLS + ks * 16);
             asm volatile("{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n"
                          :: "r"(dcol[t]), "r"(ahi), "l"(bd), "r"(idesc[t]), "r"(acc0));
             asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, 1;"
@@ -337,12 +333,12 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
     if (tid == 0) {
         abort_flag = 0;
         for (int s = 0; s < NSTAGE; ++s) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_full[s])), "r"(PWARPS / 2));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_full[s])), "r"(PWARPS));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_empty[s])), "r"(1));
         }
         for (int b = 0; b < NFBUF; ++b) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_ffull[b])), "r"(1));
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_fempty[b])), "r"(PWARPS / 2));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_fempty[b])), "r"(PWARPS));
         }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_seg)), "r"(1));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_drained)), "r"(PWARPS));
@@ -364,30 +360,35 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
 
     if (warp < PWARPS) {
         // ================= producers =================
-        // Two groups of 8 warps take alternate chunks (group g: chunks c with
-        // c % 2 == g, A / B stage g), so one group's shared-memory loads overlap
-        // the other's arithmetic.  Warp w of a group owns TMEM lane quarter
-        // q = w % 4 of the tile pair p = (w % 8) / 4 (tiles 2p and 2p + 1).
-        // Lane 4x + a: x is one of the warp's 8 row threads, each with two
-        // slots; slot u lies in tile 2p + u and holds the pair rows
-        // (i_u, J_u + y), y = 0..3, at TMEM lanes 32q + x + 8y.  Lane a forms
-        // voxels 4a .. 4a+3 of every 16-voxel k-step of those 8 rows.  The
-        // plan gives both slots the same run J wherever it can, so a thread
-        // loads 6 field pieces per k-step for its 32 products.
+        // All 16 warps work on every chunk (A / B stage c % 2).  Warp w owns
+        // TMEM lane quarter q = w % 4 of the tile pair p = (w / 4) % 2 (tiles
+        // 2p and 2p + 1) in k-step w / 8.  Lane 4x + a: x is one of the warp's
+        // 8 row threads, each with two slots; slot u lies in tile 2p + u and
+        // holds the pair rows (i_u, J_u + y), y = 0..3, at TMEM lanes
+        // 32q + x + 8y.  Lane a forms voxels 4a .. 4a+3 of the warp's 16-voxel
+        // k-step of those 8 rows.  The plan gives both slots the same run J
+        // wherever it can, so a thread loads 6 field pieces for its 32
+        // products.  With two A stages a chunk's A can be written only after
+        // the MMAs of the chunk two back complete, so the tensor pipe stays
+        // busy only if one chunk is produced within one chunk's MMA time:
+        // spreading each chunk over all 16 warps (half a chunk's k-steps per
+        // warp) keeps the production of a chunk short.
         const int rows = G.rows;
         const int nsh = P.nshell;
-        const int grp = warp >> 3;
-        const int gtid = tid & 255;                   // thread index within the group
-        const int tp = (warp & 7) >> 2;
+        const int gtid = tid;
+        const int tp = (warp >> 2) & 1;
+        const int kstep = (warp >> 3) & 1;            // warp-uniform
+        const uint32_t kx = kstep ? 64u : 0u;
         const bool tp_on = 2 * tp < G.ntiles;         // warp-uniform
         const int ax = lane & 3;
         const uint32_t code =
             (uint32_t)P.rt_tab[(size_t)blockIdx.y * RT_PER_GROUP + tp * 32 + q * 8 + (lane >> 2)];
-        // byte offset of this lane's 16-byte piece of field row r in k-step 0
-        // (k-step 1: XOR 64, the other half of the 128-byte swizzled row)
+        // byte offset of this lane's 16-byte piece of field row r in the
+        // warp's k-step (k-step 1: XOR 64, the other half of the 128-byte
+        // swizzled row)
         auto foff = [&](int r) {
             r = min(r, nsh - 1);
-            return (uint32_t)(r * 128 + ((ax ^ (r & 7)) << 4));
+            return (uint32_t)(r * 128 + ((ax ^ (r & 7)) << 4)) ^ kx;
         };
         const uint32_t oi0 = foff((int)(code & 0xffu)), oi1 = foff((int)((code >> 8) & 0xffu));
         const int J0 = (int)((code >> 16) & 0xffu), J1 = (int)(code >> 24);
@@ -395,8 +396,9 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
         uint32_t oj0[4];
 #pragma unroll
         for (int y = 0; y < 4; ++y) oj0[y] = foff(J0 + y);
-        // B writer: shell r, k-group g (voxels 8g..8g+7); 4 nshell <= 256 threads per group
+        // B writer: shell r, k-group g (voxels 8g..8g+7); 4 nshell <= 512 threads
         int ub_r = -1, ub_g = 0;
+        const bool b_warp = (warp * 32) < nsh * 4;    // warp-uniform
         if (gtid < nsh * 4) {
             ub_g = (gtid >= nsh) + (gtid >= 2 * nsh) + (gtid >= 3 * nsh);
             ub_r = gtid - ub_g * nsh;
@@ -442,14 +444,14 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
             ++seg_count;
             return true;
         };
-        for (int c = grp; c < nch; c += 2) {
+        for (int c = 0; c < nch; ++c) {
             if (__any_sync(0xffffffffu, abort_flag != 0)) { failed = true; break; }   // warp-uniform exit
             // segments that ended before this chunk are drained first
             while (seg_count < nseg && (seg_count + 1) * SEG - 1 < c) {
                 if (!drain()) { atomicExch(P.err, 2); abort_flag = 1; failed = true; break; }
             }
             if (failed) break;
-            const int s = grp;                        // == c & 1
+            const int s = c & 1;
             const int b = c % NFBUF;
             if (!warp_wait(smem_u32(&bar_ffull[b]), (uint32_t)(c / NFBUF) & 1u)) {
                 atomicExch(P.err, 1);
@@ -476,31 +478,26 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
                                      make_float2(e.z, e.w)};
                 split_store8(x, Bst + op_off(brow(ub_r, 0), ub_g), Bst + op_off(brow(ub_r, 1), ub_g));
             }
-            // A operand: this thread's 8 pair rows x 4 voxels per k-step, straight into TMEM
+            // A operand: this thread's 8 pair rows x 4 voxels of its k-step, straight into TMEM
             if (tp_on) {
-                float4 fi0[2], fi1[2], fj[2][4];
+                const float4 fi0 = lds4(F, oi0);
+                float4 fj[4];
 #pragma unroll
-                for (int ks = 0; ks < KC / 16; ++ks) {
-                    const uint32_t kx = ks ? 64u : 0u;
-                    fi0[ks] = lds4(F, oi0 ^ kx);
-#pragma unroll
-                    for (int y = 0; y < 4; ++y) fj[ks][y] = lds4(F, oj0[y] ^ kx);
-                }
-                store_slot(fi0, fj, lane_base + acol(s, 2 * tp, 0));
-                fi1[0] = lds4(F, oi1);
-                fi1[1] = lds4(F, oi1 ^ 64u);
+                for (int y = 0; y < 4; ++y) fj[y] = lds4(F, oj0[y]);
+                const float4 fi1 = lds4(F, oi1);
+                store_slot(fi0, fj, lane_base + acol(s, 2 * tp, kstep));
                 if (reload) {
 #pragma unroll
-                    for (int ks = 0; ks < KC / 16; ++ks)
-#pragma unroll
-                        for (int y = 0; y < 4; ++y) fj[ks][y] = lds4(F, foff(J1 + y) ^ (ks ? 64u : 0u));
+                    for (int y = 0; y < 4; ++y) fj[y] = lds4(F, foff(J1 + y));
                 }
-                store_slot(fi1, fj, lane_base + acol(s, 2 * tp + 1, 0));
+                store_slot(fi1, fj, lane_base + acol(s, 2 * tp + 1, kstep));
             }
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            // B writes (generic proxy) made visible to the MMA (async proxy):
+            // only the warps that hold B writers need the fence
+            if (b_warp) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            // one arrive per warp (the barriers count the 8 warps of a group):
+            // one arrive per warp (the barriers count the 16 producer warps):
             // the lanes' writes and reads are ordered before lane 0's release
             __syncwarp();
             if (lane == 0) {
@@ -515,8 +512,7 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
     } else if (warp == MMA_WARP) {
         if (lane == 0) {
             // ================= MMA issuer =================
-            // Every operand address is computed once: B descriptors per
-            // (stage, k-step), A TMEM addresses per (stage, k-step, tile).
+            // Operand addresses: per chunk a stage base plus constant offsets.
             const int ntiles = G.ntiles;
             const bool wide = G.wide != 0;
             uint32_t idesc[MAXTILES], dcol[MAXTILES];
@@ -526,20 +522,10 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
                 dcol[t] = tmem + (uint32_t)G.tile_col[t];
             }
             const uint32_t sbase = smem_u32(stage_base);
-            // B descriptors: wide form all rows (8-row blocks 512 bytes
-            // apart); narrow form the hi blocks only (1024 apart; the lo
-            // blocks are 512 bytes further)
-            uint64_t bdesc[NSTAGE][KC / 16];
-            uint32_t aad[NSTAGE][KC / 16][MAXTILES];
-#pragma unroll
-            for (int s = 0; s < NSTAGE; ++s)
-#pragma unroll
-                for (int ks = 0; ks < KC / 16; ++ks) {
-                    bdesc[s][ks] = make_desc(sbase + (uint32_t)(s * STAGE_BYTES) + (uint32_t)(ks * 256), 128,
-                                             wide ? 512 : 1024);
-#pragma unroll
-                    for (int t = 0; t < MAXTILES; ++t) aad[s][ks][t] = tmem + acol(s, t, ks);
-                }
+            // B descriptor of stage 0, k-step 0: wide form all rows (8-row
+            // blocks 512 bytes apart); narrow form the hi blocks only (1024
+            // apart; the lo blocks are 512 bytes further)
+            const uint64_t bdesc0 = make_desc(sbase, 128, wide ? 512 : 1024);
             const int mode = (wide ? 2 : 0) + (ntiles > 2 ? 1 : 0);
             int seg_count = 0;
             uint32_t first = 0;   // 0: the next MMA of each tile overwrites its accumulator
@@ -549,11 +535,13 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 // one branch-free MMA sequence per (form, tile count): a
                 // branch between the MMAs of a chunk slows their issue by ~30 %
+                const uint32_t abase = tmem + acol(s, 0, 0);
+                const uint64_t bd0 = bdesc0 + (uint64_t)((s * STAGE_BYTES) >> 4);
                 switch (mode) {
-                    case 0: issue_chunk<false, 2>(dcol, aad, bdesc, idesc, s, first); break;
-                    case 1: issue_chunk<false, 4>(dcol, aad, bdesc, idesc, s, first); break;
-                    case 2: issue_chunk<true, 2>(dcol, aad, bdesc, idesc, s, first); break;
-                    default: issue_chunk<true, 4>(dcol, aad, bdesc, idesc, s, first); break;
+                    case 0: issue_chunk<false, 2>(dcol, abase, bd0, idesc, first); break;
+                    case 1: issue_chunk<false, 4>(dcol, abase, bd0, idesc, first); break;
+                    case 2: issue_chunk<true, 2>(dcol, abase, bd0, idesc, first); break;
+                    default: issue_chunk<true, 4>(dcol, abase, bd0, idesc, first); break;
                 }
                 first = 1u;
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
