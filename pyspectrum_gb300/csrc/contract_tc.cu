@@ -446,11 +446,6 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
         };
         for (int c = 0; c < nch; ++c) {
             if (__any_sync(0xffffffffu, abort_flag != 0)) { failed = true; break; }   // warp-uniform exit
-            // segments that ended before this chunk are drained first
-            while (seg_count < nseg && (seg_count + 1) * SEG - 1 < c) {
-                if (!drain()) { atomicExch(P.err, 2); abort_flag = 1; failed = true; break; }
-            }
-            if (failed) break;
             const int s = c & 1;
             const int b = c % NFBUF;
             if (!warp_wait(smem_u32(&bar_ffull[b]), (uint32_t)(c / NFBUF) & 1u)) {
@@ -504,6 +499,13 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
                 mbar_arrive(smem_u32(&bar_full[s]));
                 mbar_arrive(smem_u32(&bar_fempty[b]));
             }
+            // a segment that ended before this chunk is drained after the
+            // chunk is produced: its MMAs (which wait for the drain) can then
+            // start as soon as the drain ends
+            while (seg_count < nseg && (seg_count + 1) * SEG - 1 < c) {
+                if (!drain()) { atomicExch(P.err, 2); abort_flag = 1; failed = true; break; }
+            }
+            if (failed) break;
         }
         // the remaining segments (the last one ends with the last chunk)
         while (!failed && seg_count < nseg) {
