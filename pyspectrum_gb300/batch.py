@@ -114,12 +114,12 @@ class BkBatch:
                 xyz_d.record_stream(cur)
             pending = self._upload(mocks[idx + 1][0]) if idx + 1 < len(mocks) else None
             npart = xyz_d.shape[1]
-            w_np = np.ones(npart) if w is None else np.asarray(w, dtype=np.float64)
-            nbar = float(np.sum(w_np)) / L ** 3
-            w_d = None if w is None else torch.as_tensor(w_np, device=self.device)
+            wsum = float(npart) if w is None else float(np.sum(np.asarray(w, dtype=np.float64)))
+            nbar = wsum / L ** 3
+            w_d = None if w is None else torch.as_tensor(np.asarray(w, dtype=np.float64), device=self.device)
             geo = self.geometry(n)
             xyzs, ws = core.prepare_positions(xyz_d, L, w_d)
-            core.fft_periodic_half(xyzs, ws, n, L, float(np.sum(w_np)), grid=geo.grid, half=geo.half)
+            core.fft_periodic_half(xyzs, ws, n, L, wsum, grid=geo.grid, half=geo.half)
             geo.device_part()
             geo.plan.normalize(True, nbar, kf)
             host = torch.empty(geo.plan.out.shape, dtype=torch.float64, pin_memory=True)

@@ -49,7 +49,10 @@ def positions_to_device(xyz, device=None) -> torch.Tensor:
     t = torch.as_tensor(xyz)
     if t.dim() != 2 or t.shape[0] != 3:
         raise ValueError("positions must be a 3 x N array")
-    return t.to(device=device, dtype=torch.float64).contiguous()
+    # from page-locked memory the copy is queued on the stream (every public
+    # entry point reads its result back, which orders it before return)
+    pinned = t.device.type == "cpu" and t.is_pinned() and t.dtype == torch.float64
+    return t.to(device=device, dtype=torch.float64, non_blocking=pinned).contiguous()
 
 
 def prepare_positions(xyz_d: torch.Tensor, Lbox: float, w_d=None, vel_d=None, los: int = 2,
@@ -68,6 +71,20 @@ def prepare_positions(xyz_d: torch.Tensor, Lbox: float, w_d=None, vel_d=None, lo
     return xyzs, ws
 
 
+_grids: dict = {}
+
+
+def _assign_grid(n: int, device) -> torch.Tensor:
+    """The interlaced assignment grid (N^3 complex64), kept per device and N:
+    it is scratch, fully rewritten by every call on the same stream."""
+    key = (n, str(device))
+    g = _grids.get(key)
+    if g is None:
+        g = torch.empty((n, n, n), dtype=torch.complex64, device=device)
+        _grids[key] = g
+    return g
+
+
 def fft_periodic_half(xyzs: torch.Tensor, ws, Ngrid: int, Lbox: float, wsum: float,
                       grid: torch.Tensor | None = None, half: torch.Tensor | None = None) -> torch.Tensor:
     """FFT_periodic (pyspectrum.py:909-959) on device: assign -> FFT -> fcomb.
@@ -75,9 +92,8 @@ def fft_periodic_half(xyzs: torch.Tensor, ws, Ngrid: int, Lbox: float, wsum: flo
     n = int(Ngrid)
     dev = xyzs.device
     if grid is None:
-        grid = torch.zeros((n, n, n), dtype=torch.complex64, device=dev)
-    else:
-        grid.zero_()
+        grid = _assign_grid(n, dev)
+    grid.zero_()
     kf_ks = float(np.float32(float(n) / Lbox))          # pyspectrum.py:931
     call("pyspec_assign_pcs_interlaced", ptr(xyzs), ptr(ws), xyzs.shape[1], n, kf_ks, 0.0,
          ptr(grid), stream_ptr())
@@ -274,8 +290,9 @@ def get_plan(Ngrid, step, Ncut, Nmax, method="fp32", device=None) -> BkPlan:
 
 
 def release_plans():
-    """Drop cached plans (and their device buffers)."""
+    """Drop cached plans and scratch grids (and their device buffers)."""
     _plans.clear()
+    _grids.clear()
 
 
 # ---------------------------------------------------------------------------

@@ -37,8 +37,11 @@ __all__ = ["FFT_periodic", "FFTperiodic", "reflect_delta", "Pk_periodic", "Pk_pe
            "applyRSD", "Bk_periodic_batch", "B0_survey", "_B0_survey", "FFT_survey_mono"]
 
 
-def _np_weights(w, n):
-    return np.ones(n) if w is None else np.asarray(w, dtype=np.float64)
+def _weight_sum(w, n):
+    """Sum of the weights as float64 (the reference sums a float64 weight
+    array, pyspectrum.py:921-925); unit weights sum to n exactly, so no array
+    is built for them."""
+    return float(n) if w is None else float(np.sum(np.asarray(w, dtype=np.float64)))
 
 
 def _half_to_numpy(half: torch.Tensor) -> np.ndarray:
@@ -58,23 +61,23 @@ def _delta_half_device(xyz, w, Lbox, Ngrid, vel=None, los=2, rsd_factor=0.0, dev
         raise ValueError("empty catalogue: the density contrast needs at least one object")
     if int(Ngrid) < 4 or int(Ngrid) % 2:
         raise ValueError("Ngrid must be even and >= 4")
-    if w is not None and float(np.sum(np.asarray(w, dtype=np.float64))) == 0.0:
+    wsum = _weight_sum(w, npart)
+    if wsum == 0.0:
         raise ValueError("the weights sum to zero (the density is normalised by their sum)")
     dev = core._dev(device)
-    w_np = _np_weights(w, npart)
     xyz_d = core.positions_to_device(xyz, dev)
-    w_d = None if w is None else torch.as_tensor(w_np, device=dev)
+    w_d = None if w is None else torch.as_tensor(np.asarray(w, dtype=np.float64), device=dev)
     v_d = None if vel is None else core.positions_to_device(vel, dev)
     xyzs, ws = core.prepare_positions(xyz_d, Lbox, w_d, v_d, los, rsd_factor)
-    return core.fft_periodic_half(xyzs, ws, Ngrid, Lbox, float(np.sum(w_np))), npart, w_np
+    return core.fft_periodic_half(xyzs, ws, Ngrid, Lbox, wsum), npart, wsum
 
 
 def FFT_periodic(xyz, w=None, Lbox=2600., Ngrid=360, fft='pyfftw', silent=True, device=None):
     """pyspectrum.py:909-959: particles -> half-complex delta(k), shape
     (Ngrid//2+1, Ngrid, Ngrid) complex64, indexed [x, y, z]."""
-    half, npart, w_np = _delta_half_device(xyz, w, Lbox, Ngrid, device=device)
+    half, npart, wsum = _delta_half_device(xyz, w, Lbox, Ngrid, device=device)
     if not silent:
-        print('%i positions, Ntot=%.f' % (npart, np.sum(w_np)))
+        print('%i positions, Ntot=%.f' % (npart, wsum))
     return _half_to_numpy(half)
 
 
@@ -147,15 +150,14 @@ def Bk_periodic(xyz, w=None, Lbox=2600, Ngrid=360, step=3, Ncut=3, Nmax=40, fft=
     'i_k2', 'i_k3', 'p0k1', 'p0k2', 'p0k3', 'b123', 'q123', 'counts',
     'p0k_sn', 'b123_sn'."""
     N = np.asarray(xyz).shape[1] if not torch.is_tensor(xyz) else xyz.shape[1]
-    w_np = _np_weights(w, N)
-    nbar = np.sum(w_np) / Lbox ** 3
+    half, _, wsum = _delta_half_device(xyz, w, Lbox, Ngrid, device=device)
+    nbar = wsum / Lbox ** 3
     kf = 2 * np.pi / Lbox
     if not silent:
         print('------------------')
         print('%i positions in %i box' % (N, Lbox))
-        print('sum w_i = %f' % np.sum(w_np))
+        print('sum w_i = %f' % wsum)
         print('nbar = %f' % nbar)
-    half, _, _ = _delta_half_device(xyz, w, Lbox, Ngrid, device=device)
     bispec = _bk_from_half(half, Ngrid, step, Ncut, Nmax, method, units=(nbar, kf), device=device)
     bispec['meta'] = {'Lbox': Lbox, 'Ngrid': Ngrid, 'step': step, 'Ncut': Ncut, 'Nmax': Nmax, 'N': N,
                       'nbar': nbar, 'kf': kf}
@@ -212,8 +214,8 @@ def Pk_periodic_rsd(xyz, w=None, Lbox=2600, Ngrid=360, rsd=2, Nmubin=10, fft='py
 def Pk_periodic(xyz, w=None, Lbox=2600, Ngrid=360, fft='pyfftw', silent=True, device=None):
     """pyspectrum.py:644-728: monopole in k_f-wide bins.  Keys 'meta', 'k',
     'p0k', 'counts', 'p0k_sn'."""
-    half, N, w_np = _delta_half_device(xyz, w, Lbox, Ngrid, device=device)
-    nbar = np.sum(w_np) / Lbox ** 3
+    half, N, wsum = _delta_half_device(xyz, w, Lbox, Ngrid, device=device)
+    nbar = wsum / Lbox ** 3
     kf = 2 * np.pi / Lbox
     k, p0k, counts = core.pk_monopole(half, Lbox)
     return {'meta': {'Lbox': Lbox, 'Ngrid': Ngrid, 'N': N, 'nbar': nbar, 'kf': kf},
@@ -227,12 +229,10 @@ def Bk_periodic_rsd(xyz, vxyz, redshift, h=0.7, omega0_m=0.3, LOS='z', w=None, L
     holds 'pk', the Pk_periodic_rsd dictionary (P0, P2, P4, P(k, mu)) of the
     same redshift-space grid.  The reference has no function of this name."""
     los = {'x': 0, 'y': 1, 'z': 2}[LOS]
-    N = np.asarray(xyz).shape[1] if not torch.is_tensor(xyz) else xyz.shape[1]
-    w_np = _np_weights(w, N)
-    nbar = np.sum(w_np) / Lbox ** 3
+    half, N, wsum = _delta_half_device(xyz, w, Lbox, Ngrid, vel=vxyz, los=los,
+                                       rsd_factor=core.rsd_factor(redshift, omega0_m), device=device)
+    nbar = wsum / Lbox ** 3
     kf = 2 * np.pi / Lbox
-    half, _, _ = _delta_half_device(xyz, w, Lbox, Ngrid, vel=vxyz, los=los,
-                                    rsd_factor=core.rsd_factor(redshift, omega0_m), device=device)
     bispec = _bk_from_half(half, Ngrid, step, Ncut, Nmax, method, units=(nbar, kf), device=device)
     bispec['meta'] = {'Lbox': Lbox, 'Ngrid': Ngrid, 'step': step, 'Ncut': Ncut, 'Nmax': Nmax, 'N': N,
                       'nbar': nbar, 'kf': kf, 'redshift': redshift, 'h': h, 'omega0_m': omega0_m, 'LOS': LOS}
