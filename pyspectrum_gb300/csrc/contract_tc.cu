@@ -48,6 +48,7 @@
 #include <cuda_bf16.h>
 #include <string.h>
 #include <algorithm>
+#include <array>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -71,6 +72,7 @@ constexpr int SEG = 32;              // chunks between accumulator drains (TMEM 
 constexpr int MAXGROUPS = 8;
 constexpr int MAXTILES = 4;
 constexpr int RT_PER_GROUP = 64;     // producer row threads per group: 2 tile pairs x 4 lane quarters x 8
+constexpr int RT_WORDS = 3;          // int32 words per row thread in the row-thread table
 constexpr int ACOLS = 32;            // TMEM columns of one tile's A operand per stage (2 k-steps x (8 hi + 8 lo))
 constexpr int NFBUF = 6;             // field buffers in the copy ring
 constexpr unsigned long long kWaitNs = 2000000000ull;   // 2 s bound on any mbarrier wait
@@ -102,8 +104,9 @@ struct Params {
     // rows), lmin, lmax (the columns l of its triangles) and the first of its
     // Kahan slots; the row's columns l in [lmin, lmax] own consecutive slots
     const int16_t* pair_row;
-    // [group][64] per producer row thread: i0 | i1 << 8 | J0 << 16 | J1 << 24,
-    // its slots u = 0, 1: pair rows (i_u, J_u + y), y = 0..3
+    // [group][64][3] per producer row thread: word 0 = i0 | i1 << 8, words
+    // 1 and 2 = the four shells g_{u,y} of slot u (byte y); slot u holds the
+    // pair rows (i_u, g_{u,y}), y = 0..3
     const int32_t* rt_tab;
     const int32_t* slot_tri;     // [group][maxslots] triangle index of each slot (-1: unused)
     double* partials;            // [gridDim.x][ntri]
@@ -380,9 +383,11 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
         const int kstep = (warp >> 3) & 1;            // warp-uniform
         const uint32_t kx = kstep ? 64u : 0u;
         const bool tp_on = 2 * tp < G.ntiles;         // warp-uniform
+        const bool slot1_on = 2 * tp + 1 < G.ntiles;  // warp-uniform (a 3-tile plan has no tile 3)
         const int ax = lane & 3;
-        const uint32_t code =
-            (uint32_t)P.rt_tab[(size_t)blockIdx.y * RT_PER_GROUP + tp * 32 + q * 8 + (lane >> 2)];
+        const int32_t* rtw = P.rt_tab + ((size_t)blockIdx.y * RT_PER_GROUP + tp * 32 + q * 8 + (lane >> 2)) * RT_WORDS;
+        const uint32_t code = (uint32_t)rtw[0];
+        const uint32_t gs0 = (uint32_t)rtw[1], gs1 = (uint32_t)rtw[2];
         // byte offset of this lane's 16-byte piece of field row r in the
         // warp's k-step (k-step 1: XOR 64, the other half of the 128-byte
         // swizzled row)
@@ -391,11 +396,10 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
             return (uint32_t)(r * 128 + ((ax ^ (r & 7)) << 4)) ^ kx;
         };
         const uint32_t oi0 = foff((int)(code & 0xffu)), oi1 = foff((int)((code >> 8) & 0xffu));
-        const int J0 = (int)((code >> 16) & 0xffu), J1 = (int)(code >> 24);
-        const bool reload = J1 != J0;
+        const bool reload = gs1 != gs0;
         uint32_t oj0[4];
 #pragma unroll
-        for (int y = 0; y < 4; ++y) oj0[y] = foff(J0 + y);
+        for (int y = 0; y < 4; ++y) oj0[y] = foff((int)((gs0 >> (8 * y)) & 0xffu));
         // B writer: shell r, k-group g (voxels 8g..8g+7); 4 nshell <= 512 threads
         int ub_r = -1, ub_g = 0;
         const bool b_warp = (warp * 32) < nsh * 4;    // warp-uniform
@@ -473,19 +477,21 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
                                      make_float2(e.z, e.w)};
                 split_store8(x, Bst + op_off(brow(ub_r, 0), ub_g), Bst + op_off(brow(ub_r, 1), ub_g));
             }
-            // A operand: this thread's 8 pair rows x 4 voxels of its k-step, straight into TMEM
+            // A operand: this thread's 8 (or 4) pair rows x 4 voxels of its k-step, straight into TMEM
             if (tp_on) {
                 const float4 fi0 = lds4(F, oi0);
                 float4 fj[4];
 #pragma unroll
                 for (int y = 0; y < 4; ++y) fj[y] = lds4(F, oj0[y]);
-                const float4 fi1 = lds4(F, oi1);
                 store_slot(fi0, fj, lane_base + acol(s, 2 * tp, kstep));
-                if (reload) {
+                if (slot1_on) {
+                    const float4 fi1 = lds4(F, oi1);
+                    if (reload) {
 #pragma unroll
-                    for (int y = 0; y < 4; ++y) fj[y] = lds4(F, foff(J1 + y));
+                        for (int y = 0; y < 4; ++y) fj[y] = lds4(F, foff((int)((gs1 >> (8 * y)) & 0xffu)));
+                    }
+                    store_slot(fi1, fj, lane_base + acol(s, 2 * tp + 1, kstep));
                 }
-                store_slot(fi1, fj, lane_base + acol(s, 2 * tp + 1, kstep));
             }
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
             // B writes (generic proxy) made visible to the MMA (async proxy):
@@ -528,7 +534,8 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
             // blocks 512 bytes apart); narrow form the hi blocks only (1024
             // apart; the lo blocks are 512 bytes further)
             const uint64_t bdesc0 = make_desc(sbase, 128, wide ? 512 : 1024);
-            const int mode = (wide ? 2 : 0) + (ntiles > 2 ? 1 : 0);
+            // tile count 2, 3 or 4 and the form select one branch-free sequence
+            const int mode = (wide ? 3 : 0) + (ntiles == 2 ? 0 : ntiles == 3 ? 1 : 2);
             int seg_count = 0;
             uint32_t first = 0;   // 0: the next MMA of each tile overwrites its accumulator
             for (int c = 0; c < nch; ++c) {
@@ -541,8 +548,10 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
                 const uint64_t bd0 = bdesc0 + (uint64_t)((s * STAGE_BYTES) >> 4);
                 switch (mode) {
                     case 0: issue_chunk<false, 2>(dcol, abase, bd0, idesc, first); break;
-                    case 1: issue_chunk<false, 4>(dcol, abase, bd0, idesc, first); break;
-                    case 2: issue_chunk<true, 2>(dcol, abase, bd0, idesc, first); break;
+                    case 1: issue_chunk<false, 3>(dcol, abase, bd0, idesc, first); break;
+                    case 2: issue_chunk<false, 4>(dcol, abase, bd0, idesc, first); break;
+                    case 3: issue_chunk<true, 2>(dcol, abase, bd0, idesc, first); break;
+                    case 4: issue_chunk<true, 3>(dcol, abase, bd0, idesc, first); break;
                     default: issue_chunk<true, 4>(dcol, abase, bd0, idesc, first); break;
                 }
                 first = 1u;
@@ -661,6 +670,232 @@ static int phase_conflicts(const RowThread& A, const RowThread& B) {
     return c;
 }
 
+// Slot table and the device image of a plan whose rows and row threads are set.
+static void finish_plan(HostPlan* hp, int ngroups, int maxslots, const std::vector<std::vector<int32_t>>& gslots,
+                        size_t fixed) {
+    Params& P = hp->base;
+    P.maxslots = maxslots;
+    hp->slot_tri.assign((size_t)ngroups * maxslots, -1);
+    for (int g = 0; g < ngroups; ++g)
+        for (size_t i = 0; i < gslots[g].size(); ++i) hp->slot_tri[(size_t)g * maxslots + i] = gslots[g][i];
+    hp->smem = fixed + sizeof(float2) * (size_t)maxslots;
+    hp->off_rt = al256(hp->pair_row.size() * 2);
+    hp->off_stri = hp->off_rt + al256(hp->rt_tab.size() * 4);
+    hp->image.assign(hp->off_stri + al256(hp->slot_tri.size() * 4), 0);
+    memcpy(hp->image.data(), hp->pair_row.data(), hp->pair_row.size() * 2);
+    memcpy(hp->image.data() + hp->off_rt, hp->rt_tab.data(), hp->rt_tab.size() * 4);
+    memcpy(hp->image.data() + hp->off_stri, hp->slot_tri.data(), hp->slot_tri.size() * 4);
+    hp->image_src = pinned_copy(hp->image.data(), hp->image.size());
+    if (hp->image_src == nullptr) hp->image_src = hp->image.data();
+    hp->ok = true;
+}
+
+// Cover plan: a D row (a, b) gives B(a, b, c) for every column c, so the rows
+// need only be a set of shell pairs that meets every triangle, not the pairs
+// of its two largest shells.  Rows come in blocks that match the producer
+// threads: up to 32 "two-slot" blocks {f1, f2} x {g0..g3} (tiles 0 and 1,
+// one load of each g serves both slots) chosen greedily by triangles newly
+// covered, then up to 32 "one-slot" blocks {f} x {g0..g3} (tile 2).  When
+// they cover every triangle the contraction runs on 3 tiles instead of 4:
+// 12 MMAs per chunk instead of 16 (Nmax 40: 32 + 29 blocks, 372 rows, against
+// 440 pairs + padding).  Returns false (and leaves hp untouched) otherwise.
+static bool build_cover_plan(HostPlan* hp, int nshell, const int32_t* tri_host, int ntri, int budget, size_t fixed) {
+    const int S = nshell, T = ntri, W = (T + 63) / 64;
+    std::vector<std::array<int, 3>> tri(T);
+    for (int t = 0; t < T; ++t) {
+        int v[3] = {tri_host[t], tri_host[ntri + t], tri_host[2 * ntri + t]};
+        std::sort(v, v + 3);
+        tri[t] = {v[2], v[1], v[0]};
+    }
+    // pm(a, b): triangles that contain both a and b (a == b: twice)
+    std::vector<uint64_t> pm((size_t)S * S * W, 0);
+    auto PM = [&](int a, int b) { return &pm[((size_t)a * S + b) * W]; };
+    auto setbit = [&](int a, int b, int t) {
+        PM(a, b)[t >> 6] |= 1ull << (t & 63);
+        PM(b, a)[t >> 6] |= 1ull << (t & 63);
+    };
+    for (int t = 0; t < T; ++t) {
+        const int i = tri[t][0], j = tri[t][1], l = tri[t][2];
+        setbit(i, j, t);
+        setbit(i, l, t);
+        setbit(j, l, t);
+    }
+    std::vector<uint64_t> unc(W, ~0ull);
+    if (T % 64) unc[W - 1] = (1ull << (T % 64)) - 1;
+    auto remaining = [&]() {
+        for (int w = 0; w < W; ++w)
+            if (unc[w]) return true;
+        return false;
+    };
+    struct Block { int f[2]; int nf; int g[4]; };
+    std::vector<Block> blocks2, blocks1;
+    std::vector<uint64_t> cand((size_t)(S + 1) * W), m(W), best_m(W);
+    // greedy: for the f set, pick four g one at a time by newly covered triangles
+    auto grow = [&](const int* f, int nf, int* g, std::vector<uint64_t>& cov) {
+        for (int x = 0; x < S; ++x)
+            for (int w = 0; w < W; ++w) {
+                uint64_t v = 0;
+                for (int k = 0; k < nf; ++k) v |= PM(f[k], x)[w];
+                cand[(size_t)x * W + w] = v & unc[w];
+            }
+        std::fill(cov.begin(), cov.end(), 0ull);
+        int total = 0;
+        for (int pick = 0; pick < 4; ++pick) {
+            int gb = -1, cb = -1;
+            for (int x = 0; x < S; ++x) {
+                bool used = false;
+                for (int k = 0; k < pick; ++k) used |= g[k] == x;
+                if (used) continue;
+                int c = 0;
+                for (int w = 0; w < W; ++w) c += __builtin_popcountll(cand[(size_t)x * W + w] & ~cov[w]);
+                if (c > cb) { cb = c; gb = x; }
+            }
+            g[pick] = gb;
+            total += cb;
+            for (int w = 0; w < W; ++w) cov[w] |= cand[(size_t)gb * W + w];
+        }
+        return total;
+    };
+    std::vector<int> single(S);
+    std::vector<std::pair<int, std::pair<int, int>>> order;
+    for (int k = 0; k < 32 && remaining(); ++k) {
+        Block bb{{0, 0}, 2, {0, 0, 0, 0}};
+        int bc = -1;
+        // candidates in order of the sum of their shells' one-slot coverage;
+        // the scan stops once that sum cannot beat the best pair found
+        for (int f = 0; f < S; ++f) {
+            int g[4];
+            single[f] = grow(&f, 1, g, m);
+        }
+        order.clear();
+        for (int f1 = 0; f1 < S; ++f1)
+            for (int f2 = f1 + 1; f2 < S; ++f2) order.push_back({single[f1] + single[f2], {f1, f2}});
+        std::sort(order.begin(), order.end(), [](const std::pair<int, std::pair<int, int>>& x,
+                                                  const std::pair<int, std::pair<int, int>>& y) {
+            return x.first != y.first ? x.first > y.first : x.second < y.second;
+        });
+        for (const auto& o : order) {
+            if (o.first <= bc) break;
+            const int f[2] = {o.second.first, o.second.second};
+            int g[4];
+            const int c = grow(f, 2, g, m);
+            if (c > bc) {
+                bc = c;
+                bb = Block{{f[0], f[1]}, 2, {g[0], g[1], g[2], g[3]}};
+                best_m = m;
+            }
+        }
+        if (bc <= 0) break;
+        blocks2.push_back(bb);
+        for (int w = 0; w < W; ++w) unc[w] &= ~best_m[w];
+    }
+    for (int k = 0; k < 32 && remaining(); ++k) {
+        Block bb{{0, 0}, 1, {0, 0, 0, 0}};
+        int bc = -1;
+        for (int f1 = 0; f1 < S; ++f1) {
+            int g[4];
+            const int c = grow(&f1, 1, g, m);
+            if (c > bc) {
+                bc = c;
+                bb = Block{{f1, f1}, 1, {g[0], g[1], g[2], g[3]}};
+                best_m = m;
+            }
+        }
+        if (bc <= 0) break;
+        blocks1.push_back(bb);
+        for (int w = 0; w < W; ++w) unc[w] &= ~best_m[w];
+    }
+    if (remaining() || blocks1.empty()) return false;   // no cover, or no gain over 2 tiles of runs
+    // rows: two-slot block k at (q, x) = (k / 8, k % 8) in tiles 0 and 1,
+    // one-slot block k at the same positions of tile 2; row (f, g_y) at lane 32q + x + 8y
+    struct Row { int f, g; std::vector<std::pair<int, int>> cols; };   // (column, triangle)
+    std::vector<Row> rows(MAXROWS, Row{-1, -1, {}});
+    auto row_of = [](int tile, int k, int y) { return 128 * tile + 32 * (k / 8) + (k % 8) + 8 * y; };
+    for (size_t k = 0; k < blocks2.size(); ++k)
+        for (int u = 0; u < 2; ++u)
+            for (int y = 0; y < 4; ++y) rows[row_of(u, (int)k, y)] = Row{blocks2[k].f[u], blocks2[k].g[y], {}};
+    for (size_t k = 0; k < blocks1.size(); ++k)
+        for (int y = 0; y < 4; ++y) rows[row_of(2, (int)k, y)] = Row{blocks1[k].f[0], blocks1[k].g[y], {}};
+    // each triangle goes to the first row whose pair it contains; column = its third shell
+    for (int t = 0; t < T; ++t) {
+        bool done = false;
+        for (int r = 0; r < MAXROWS && !done; ++r) {
+            if (rows[r].f < 0) continue;
+            int v[3] = {tri[t][0], tri[t][1], tri[t][2]};
+            int a = -1, b = -1;
+            for (int z = 0; z < 3; ++z)
+                if (a < 0 && v[z] == rows[r].f) a = z;
+            for (int z = 0; z < 3; ++z)
+                if (b < 0 && z != a && v[z] == rows[r].g) b = z;
+            if (a < 0 || b < 0) continue;
+            rows[r].cols.push_back({v[3 - a - b], t});
+            done = true;
+        }
+        if (!done) return false;
+    }
+    Params& P = hp->base;
+    Group& G = P.g[0];
+    P.ngroups = 1;
+    P.nshell = nshell;
+    P.ntri = ntri;
+    G.ntiles = 3;
+    G.rows = 128 * G.ntiles;
+    G.table_off = 0;
+    hp->pair_row.assign((size_t)MAXROWS * 4, (int16_t)0);
+    for (int r = 0; r < MAXROWS; ++r) hp->pair_row[4 * r] = -1;
+    hp->rt_tab.assign((size_t)RT_PER_GROUP * RT_WORDS, 0);
+    auto gword = [](const int* g) {
+        return (int32_t)((uint32_t)g[0] | (uint32_t)g[1] << 8 | (uint32_t)g[2] << 16 | (uint32_t)g[3] << 24);
+    };
+    // two-slot block k: entry k (tiles 0 and 1); one-slot block k: entry
+    // 32 + k (tile 2; the warps of tile pair 1 skip slot 1, there is no tile 3)
+    for (size_t k = 0; k < blocks2.size(); ++k) {
+        int32_t* w = &hp->rt_tab[k * RT_WORDS];
+        w[0] = (int32_t)((uint32_t)blocks2[k].f[0] | (uint32_t)blocks2[k].f[1] << 8);
+        w[1] = w[2] = gword(blocks2[k].g);
+    }
+    for (size_t k = 0; k < blocks1.size(); ++k) {
+        int32_t* w = &hp->rt_tab[(32 + k) * RT_WORDS];
+        w[0] = (int32_t)((uint32_t)blocks1[k].f[0] | (uint32_t)blocks1[k].f[0] << 8);
+        w[1] = w[2] = gword(blocks1[k].g);
+    }
+    std::vector<std::vector<int32_t>> gslots(1);
+    int tile_maxl[MAXTILES] = {0, 0, 0, 0};
+    for (int r = 0; r < MAXROWS; ++r) {
+        Row& R = rows[r];
+        if (R.cols.empty()) continue;
+        std::sort(R.cols.begin(), R.cols.end());
+        const int lmin = R.cols.front().first, lmax = R.cols.back().first;
+        int16_t* pr = &hp->pair_row[(size_t)r * 4];
+        pr[0] = (int16_t)(R.f | (R.g << 8));
+        pr[1] = (int16_t)lmin;
+        pr[2] = (int16_t)lmax;
+        pr[3] = (int16_t)gslots[0].size();
+        size_t c = 0;
+        for (int l = lmin; l <= lmax; ++l) {
+            if (c < R.cols.size() && R.cols[c].first == l) gslots[0].push_back(R.cols[c++].second);
+            else gslots[0].push_back(-1);
+        }
+        tile_maxl[r / 128] = std::max(tile_maxl[r / 128], lmax);
+    }
+    if ((int)gslots[0].size() > budget || gslots[0].size() > 32767) return false;
+    int wide_cols = 0;
+    for (int t = 0; t < G.ntiles; ++t) wide_cols += 2 * ((tile_maxl[t] + 1 + 7) / 8 * 8);
+    G.wide = wide_cols <= 512 - NSTAGE * MAXTILES * ACOLS ? 1 : 0;
+    int col = 0;
+    for (int t = 0; t < MAXTILES; ++t) { G.tile_n[t] = 16; G.tile_col[t] = 0; }
+    for (int t = 0; t < G.ntiles; ++t) {
+        G.tile_n[t] = G.wide ? (tile_maxl[t] + 1 + 7) / 8 * 8 : (tile_maxl[t] + 1 + 15) / 16 * 16;
+        G.tile_col[t] = col;
+        col += (G.wide ? 2 : 1) * G.tile_n[t];
+    }
+    G.ncols = pow2_cols(col + NSTAGE * MAXTILES * ACOLS);
+    if (G.ncols > 512) return false;
+    G.nslots = (int)gslots[0].size();
+    finish_plan(hp, 1, std::max(1, G.nslots), gslots, fixed);
+    return true;
+}
+
 static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri) {
     HostPlan* hp = new HostPlan();
     Params& P = hp->base;
@@ -726,6 +961,10 @@ static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri) {
     };
     const size_t fixed = (size_t)fixed_smem(nshell);
     const int budget = (int)((227 * 1024 - 8192 - fixed) / sizeof(float2));
+    // fewer tiles with a pair cover where the run plan needs 4 (bounded search cost)
+    if (rts.size() > (size_t)RT_PER_GROUP / 2 && rts.size() <= (size_t)RT_PER_GROUP && nshell <= 48 && ntri <= 12000 &&
+        build_cover_plan(hp, nshell, tri_host, ntri, budget, fixed))
+        return hp;
     // CTA groups: up to 64 consecutive row threads and `budget` Kahan slots
     std::vector<size_t> group_first;
     {
@@ -754,7 +993,7 @@ static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri) {
     P.ntri = ntri;
     hp->pair_row.assign((size_t)ngroups * MAXROWS * 4, (int16_t)0);
     for (size_t r = 0; r < (size_t)ngroups * MAXROWS; ++r) hp->pair_row[4 * r] = -1;
-    hp->rt_tab.assign((size_t)ngroups * RT_PER_GROUP, 0);
+    hp->rt_tab.assign((size_t)ngroups * RT_PER_GROUP * RT_WORDS, 0);
     std::vector<std::vector<int32_t>> gslots(ngroups);
     int maxslots = 1;
     for (int g = 0; g < ngroups; ++g) {
@@ -786,9 +1025,13 @@ static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri) {
             for (size_t pos = 0; pos < order.size(); ++pos) {
                 const RowThread& r = blk[order[pos]];
                 const int q = (int)pos / 8, x = (int)pos % 8;
-                hp->rt_tab[(size_t)g * RT_PER_GROUP + 32 * tp + pos] =
-                    (int32_t)((uint32_t)r.s[0].i | (uint32_t)r.s[1].i << 8 | (uint32_t)r.s[0].J << 16 |
-                              (uint32_t)r.s[1].J << 24);
+                int32_t* w = &hp->rt_tab[((size_t)g * RT_PER_GROUP + 32 * tp + pos) * RT_WORDS];
+                w[0] = (int32_t)((uint32_t)r.s[0].i | (uint32_t)r.s[1].i << 8);
+                for (int u = 0; u < 2; ++u) {
+                    uint32_t gs = 0;
+                    for (int y = 0; y < 4; ++y) gs |= (uint32_t)std::min(r.s[u].J + y, nshell - 1) << (8 * y);
+                    w[1 + u] = (int32_t)gs;
+                }
                 for (int u = 0; u < 2; ++u) {
                     const int tile = 2 * tp + u;
                     for (int y = 0; y < 4; ++y) {
@@ -834,20 +1077,7 @@ static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri) {
         }
         maxslots = std::max(maxslots, G.nslots);
     }
-    P.maxslots = maxslots;
-    hp->slot_tri.assign((size_t)ngroups * maxslots, -1);
-    for (int g = 0; g < ngroups; ++g)
-        for (size_t i = 0; i < gslots[g].size(); ++i) hp->slot_tri[(size_t)g * maxslots + i] = gslots[g][i];
-    hp->smem = fixed + sizeof(float2) * (size_t)maxslots;
-    hp->off_rt = al256(hp->pair_row.size() * 2);
-    hp->off_stri = hp->off_rt + al256(hp->rt_tab.size() * 4);
-    hp->image.assign(hp->off_stri + al256(hp->slot_tri.size() * 4), 0);
-    memcpy(hp->image.data(), hp->pair_row.data(), hp->pair_row.size() * 2);
-    memcpy(hp->image.data() + hp->off_rt, hp->rt_tab.data(), hp->rt_tab.size() * 4);
-    memcpy(hp->image.data() + hp->off_stri, hp->slot_tri.data(), hp->slot_tri.size() * 4);
-    hp->image_src = pinned_copy(hp->image.data(), hp->image.size());
-    if (hp->image_src == nullptr) hp->image_src = hp->image.data();
-    hp->ok = true;
+    finish_plan(hp, ngroups, maxslots, gslots, fixed);
     return hp;
 }
 
@@ -878,7 +1108,7 @@ size_t contract_tc_ws(int64_t nvox, int nshell, int ntri) {
     // + one gap slot per row and shell) + partials + error word
     (void)nshell;
     const size_t rows = (size_t)tc::MAXGROUPS * tc::MAXROWS;
-    const size_t tables = rows * 4 * 2 + (size_t)tc::MAXGROUPS * tc::RT_PER_GROUP * 4 +
+    const size_t tables = rows * 4 * 2 + (size_t)tc::MAXGROUPS * tc::RT_PER_GROUP * tc::RT_WORDS * 4 +
                           (size_t)tc::MAXGROUPS * ((size_t)ntri + tc::MAXROWS * tc::MAXB) * 4 + 4096;
     const int64_t nchunks = (nvox + tc::KC - 1) / tc::KC;
     const size_t gx = (size_t)std::min<int64_t>(std::max<int64_t>(nchunks, 1), 1024);
