@@ -172,6 +172,22 @@ int pyspec_bk_contract(const float *fields, int ngrid, int nshell, const int32_t
                        void *workspace, size_t ws_bytes, void *stream);
 
 /* ------------------------------------------------------------------------
+ * Host-side check of the BF16X3 contraction plan of a triangle list (no GPU
+ * needed; no counterpart in the reference).  Builds (or reuses) the plan
+ * pyspec_bk_contract plans for tri_host and verifies that every triangle is
+ * read at exactly one (pair row, column) cell whose three shells are the
+ * triangle's, that each row's shells agree with the producer table, that
+ * every row lies in its group's tiles and every column below its tile's N.
+ * info (may be NULL) receives up to ninfo values: [0] CTA groups, [1] tiles
+ * of group 0, [2] 1 if the rows are a pair cover (0: runs of the triangles'
+ * two largest shells), [3] MMAs per 32 voxels summed over groups, [4] Kahan
+ * slots of group 0, [5] 1 if group 0 uses the wide MMA form.
+ * Returns 0; PYSPEC_E_INVALID / PYSPEC_E_UNSUPPORTED where the contraction
+ * would; PYSPEC_E_INVALID with a message if the plan fails the check.
+ * ---------------------------------------------------------------------- */
+int pyspec_bk_plan_check(int nshell, const int32_t *tri_host, int ntri, int64_t *info, int ninfo);
+
+/* ------------------------------------------------------------------------
  * Triangle contraction without device allocation.  This entry point has no
  * counterpart in the reference.  It is for callers that cannot allocate
  * device memory where they run -- inside another framework's

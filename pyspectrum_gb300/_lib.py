@@ -38,6 +38,7 @@ SIGNATURES = {
     "pyspec_bk_contract_workspace": (c_size, [c_int, c_int, c_int, c_int]),
     "pyspec_bk_contract": (c_int, [_P, c_int, c_int, _P, _P, c_int, c_int, _P, _P, c_size, _P]),
     "pyspec_bk_contract_noalloc": (c_int, [_P, c_int, c_int, _P, c_int, _P, _P]),
+    "pyspec_bk_plan_check": (c_int, [c_int, _P, c_int, _P, c_int]),
     "pyspec_bk_counts_workspace": (c_size, [c_int, c_int, c_int, c_int]),
     "pyspec_bk_counts": (c_int, [c_int, c_int, c_int, c_int, _P, c_int, _P, _P, _P, c_size, _P]),
     "pyspec_bk_normalize": (c_int, [_P, _P, _P, _P, _P, c_int, c_int, c_int, c_int, c_int, c_double, c_double, _P, _P]),

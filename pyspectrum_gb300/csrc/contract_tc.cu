@@ -637,6 +637,7 @@ struct HostPlan {
     size_t smem = 0;
     bool ok = false;
     bool invalid = false;         // the triangle list itself is malformed (vs. unsupported)
+    bool cover = false;           // rows are a pair cover (3 tiles), not runs
     char why[160] = {0};
 };
 
@@ -963,8 +964,10 @@ static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri) {
     const int budget = (int)((227 * 1024 - 8192 - fixed) / sizeof(float2));
     // fewer tiles with a pair cover where the run plan needs 4 (bounded search cost)
     if (rts.size() > (size_t)RT_PER_GROUP / 2 && rts.size() <= (size_t)RT_PER_GROUP && nshell <= 48 && ntri <= 12000 &&
-        build_cover_plan(hp, nshell, tri_host, ntri, budget, fixed))
+        build_cover_plan(hp, nshell, tri_host, ntri, budget, fixed)) {
+        hp->cover = true;
         return hp;
+    }
     // CTA groups: up to 64 consecutive row threads and `budget` Kahan slots
     std::vector<size_t> group_first;
     {
@@ -1207,4 +1210,74 @@ int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_
     return reduce_partials_launch(partials, gx, ntri, bsum, st);
 }
 
+// Verifies a built plan against its triangle list (see pyspec_bk_plan_check).
+static bool check_plan(const tc::HostPlan* hp, const int32_t* tri_host, int ntri, char* why, size_t nwhy) {
+    using namespace tc;
+    const Params& P = hp->base;
+    std::vector<int> seen(ntri, 0);
+    for (int g = 0; g < P.ngroups; ++g) {
+        const Group& G = P.g[g];
+        for (int r = 0; r < MAXROWS; ++r) {
+            const int16_t* pr = &hp->pair_row[((size_t)G.table_off + r) * 4];
+            if (pr[0] < 0) continue;
+            const int i = pr[0] & 0xff, j = (pr[0] >> 8) & 0xff, lmin = pr[1], lmax = pr[2];
+            const int tile = r / 128, q = (r % 128) / 32, x = r % 8, y = (r % 32) / 8;
+            const int tp = tile / 2, u = tile % 2;
+            const int32_t* w = &hp->rt_tab[((size_t)g * RT_PER_GROUP + tp * 32 + q * 8 + x) * RT_WORDS];
+            const int ri = (w[0] >> (8 * u)) & 0xff, rg = (w[1 + u] >> (8 * y)) & 0xff;
+            if (tile >= G.ntiles || ri != i || rg != j || lmin > lmax || lmax >= G.tile_n[tile] ||
+                pr[3] + (lmax - lmin) >= G.nslots) {
+                snprintf(why, nwhy, "group %d row %d: shells (%d, %d), table (%d, %d), columns [%d, %d]", g, r, i, j,
+                         ri, rg, lmin, lmax);
+                return false;
+            }
+            for (int l = lmin; l <= lmax; ++l) {
+                const int t = hp->slot_tri[(size_t)g * P.maxslots + pr[3] + (l - lmin)];
+                if (t < 0) continue;
+                if (t >= ntri) {
+                    snprintf(why, nwhy, "group %d row %d: slot holds triangle %d of %d", g, r, t, ntri);
+                    return false;
+                }
+                int a[3] = {i, j, l}, b[3] = {tri_host[t], tri_host[ntri + t], tri_host[2 * ntri + t]};
+                std::sort(a, a + 3);
+                std::sort(b, b + 3);
+                if (a[0] != b[0] || a[1] != b[1] || a[2] != b[2]) {
+                    snprintf(why, nwhy, "triangle %d read at shells (%d, %d, %d)", t, i, j, l);
+                    return false;
+                }
+                ++seen[t];
+            }
+        }
+    }
+    for (int t = 0; t < ntri; ++t)
+        if (seen[t] != 1) {
+            snprintf(why, nwhy, "triangle %d is read %d times", t, seen[t]);
+            return false;
+        }
+    return true;
+}
+
 }  // namespace pyspec
+
+extern "C" int pyspec_bk_plan_check(int nshell, const int32_t* tri_host, int ntri, int64_t* info, int ninfo) {
+    using namespace pyspec;
+    using namespace pyspec::tc;
+    PYSPEC_CHECK_ARG(tri_host != nullptr && ntri > 0, "empty or NULL triangle list");
+    PYSPEC_CHECK_ARG(nshell >= 1 && ninfo >= 0 && (info != nullptr || ninfo == 0), "bad arguments");
+    HostPlan* hp = get_plan(nshell, tri_host, ntri);
+    if (!hp->ok) {
+        set_error("%s", hp->why);
+        return hp->invalid ? PYSPEC_E_INVALID : PYSPEC_E_UNSUPPORTED;
+    }
+    char why[200];
+    if (!check_plan(hp, tri_host, ntri, why, sizeof(why))) {
+        set_error("contraction plan check failed: %s", why);
+        return PYSPEC_E_INVALID;
+    }
+    const Params& P = hp->base;
+    int64_t mma = 0;
+    for (int g = 0; g < P.ngroups; ++g) mma += (int64_t)P.g[g].ntiles * (KC / 16) * (P.g[g].wide ? 2 : 3);
+    const int64_t vals[6] = {P.ngroups, P.g[0].ntiles, hp->cover ? 1 : 0, mma, P.g[0].nslots, P.g[0].wide};
+    for (int k = 0; k < ninfo && k < 6; ++k) info[k] = vals[k];
+    return PYSPEC_OK;
+}
