@@ -43,6 +43,17 @@ SMALL_WORKLOAD = {"workload": "zeldovich-300k-192-step3-nmax40 (profiling case)"
 L2_FLUSH_BYTES = 512 << 20   # > 129 MB L2, written between timed steps
 
 
+def plan_macs_per_voxel(nmax, ncut, step):
+    """Tensor-core multiply-adds per voxel of the contraction plan for the
+    triangle loop (host-side plan query of the library)."""
+    from pyspectrum_gb300 import _lib, core as _core
+    jmin = ncut // step
+    tri = np.ascontiguousarray(_core.triangles(jmin, nmax) - jmin, dtype=np.int32)
+    info = np.zeros(7, dtype=np.int64)
+    _lib.call("pyspec_bk_plan_check", nmax - jmin + 1, tri.ctypes.data, int(tri.shape[1]), info.ctypes.data, 7)
+    return int(info[6])
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -387,12 +398,12 @@ def run_gpu(args, rank, world, local_rank):
     main = results["bf16x3"]
     # roofline of the dominant kernel: the tensor-core contraction.  Algorithmic
     # work = 2 T V useful FLOP (one FMA per triangle and voxel); executed tensor
-    # work = 2 FLOP x 2 A parts (hi, lo) x (sum over tiles of M x 2N: hi and lo
-    # B columns) x V, with 128-row tiles of N = 16, 32, 32, 48 shells.
+    # work = 2 FLOP x the plan's tensor multiply-adds per voxel (per 128-row
+    # tile: 2 A parts (hi, lo) x 2N B columns (hi, lo)) x V, from the plan the
+    # library builds for this triangle list.
     V = n ** 3
     useful = 2.0 * plans["bf16x3"].T * V
-    tiles_mn = 128 * 2 * (16 + 32 + 32 + 48)
-    executed = 2.0 * 2 * tiles_mn * V
+    executed = 2.0 * plan_macs_per_voxel(nmax, ncut, step) * V
     t_con = main["stage_ms"]["contraction"] / 1e3
     roofline = {"kernel": "contract_tc_kernel (+ partial reduction)", "bound": "tensor",
                 "achieved": useful / t_con / 1e12, "peak": bf16, "unit": "TFLOP/s",

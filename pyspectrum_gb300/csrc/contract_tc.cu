@@ -1275,9 +1275,14 @@ extern "C" int pyspec_bk_plan_check(int nshell, const int32_t* tri_host, int ntr
         return PYSPEC_E_INVALID;
     }
     const Params& P = hp->base;
-    int64_t mma = 0;
-    for (int g = 0; g < P.ngroups; ++g) mma += (int64_t)P.g[g].ntiles * (KC / 16) * (P.g[g].wide ? 2 : 3);
-    const int64_t vals[6] = {P.ngroups, P.g[0].ntiles, hp->cover ? 1 : 0, mma, P.g[0].nslots, P.g[0].wide};
-    for (int k = 0; k < ninfo && k < 6; ++k) info[k] = vals[k];
+    int64_t mma = 0, macs = 0;
+    for (int g = 0; g < P.ngroups; ++g) {
+        const Group& G = P.g[g];
+        mma += (int64_t)G.ntiles * (KC / 16) * (G.wide ? 2 : 3);
+        // tensor MACs per voxel: per tile M = 128 rows x (2 MMAs x 2N columns, or 3 x N)
+        for (int t = 0; t < G.ntiles; ++t) macs += 128 * (G.wide ? 2 * 2 * G.tile_n[t] : 3 * G.tile_n[t]);
+    }
+    const int64_t vals[7] = {P.ngroups, P.g[0].ntiles, hp->cover ? 1 : 0, mma, P.g[0].nslots, P.g[0].wide, macs};
+    for (int k = 0; k < ninfo && k < 7; ++k) info[k] = vals[k];
     return PYSPEC_OK;
 }

@@ -14,9 +14,9 @@ from pyspectrum_gb300 import _lib, core
 
 def plan_check(nshell, tri):
     tri = np.ascontiguousarray(tri, dtype=np.int32)
-    info = np.zeros(6, dtype=np.int64)
-    _lib.call("pyspec_bk_plan_check", int(nshell), tri.ctypes.data, int(tri.shape[1]), info.ctypes.data, 6)
-    return dict(zip(["groups", "tiles", "cover", "mma", "slots", "wide"], info.tolist()))
+    info = np.zeros(7, dtype=np.int64)
+    _lib.call("pyspec_bk_plan_check", int(nshell), tri.ctypes.data, int(tri.shape[1]), info.ctypes.data, 7)
+    return dict(zip(["groups", "tiles", "cover", "mma", "slots", "wide", "macs"], info.tolist()))
 
 
 @pytest.mark.parametrize("nmax", [1, 2, 10, 20, 30, 36, 40, 45, 60, 64])
@@ -30,7 +30,8 @@ def test_bench_workload_gets_three_tiles():
     """Nmax 40 (6350 triangles): 372 rows of a pair cover fit 3 tiles, so
     12 MMAs per 32 voxels instead of 16 (440 (largest, middle) pairs need 4)."""
     info = plan_check(40, core.triangles(1, 40) - 1)
-    assert info == {"groups": 1, "tiles": 3, "cover": 1, "mma": 12, "slots": info["slots"], "wide": 1}
+    assert info == {"groups": 1, "tiles": 3, "cover": 1, "mma": 12, "slots": info["slots"], "wide": 1,
+                    "macs": 3 * 128 * 2 * 2 * 40}
     info30 = plan_check(30, core.triangles(1, 30) - 1)
     assert info30["cover"] == 0 and info30["tiles"] == 4
 
