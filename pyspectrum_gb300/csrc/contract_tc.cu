@@ -17,16 +17,17 @@
 //     A_lo B_hi, A_hi B_lo; A_lo B_lo, 2^-16 of the rest, is dropped) into
 //     N columns, B_hi and B_lo read through descriptors that skip the other
 //     part's 8-row blocks.
-// Consecutive MMAs go to the same accumulator (all of one tile's MMAs of a
-// chunk back to back): alternating accumulators issues slower.
+// Per tile the MMAs issue back to back with no branch between them (a
+// data-dependent branch in the sequence slowed the issue by ~30 %).
 //
 // CTA layout (1 CTA per SM, persistent over a contiguous voxel range):
-//   warps 0-15 (512 threads): producers, two groups of 8 warps on alternate
-//     chunks of KC = 32 voxels.  Warp w of a group owns TMEM lane quarter
-//     w % 4 of the tile pair (w % 8) / 4.  Each thread forms 4 voxels of 8
-//     pair rows (two runs of four rows that share their shells j), splits the
-//     products into hi/lo bf16 and writes them straight into TMEM
-//     (tcgen05.st, 16x256b shape) as the MMA's A operand; threads < 4*nshell
+//   warps 0-15 (512 threads): producers, all on every chunk of KC = 32
+//     voxels.  Warp w owns TMEM lane quarter w % 4 of the tile pair
+//     (w / 4) % 2 in k-step w / 8.  Each thread forms 4 voxels of 8 pair rows
+//     (two slots of four rows that share their shells g; 4 rows where the
+//     tile pair has one tile), splits the products into hi/lo bf16 and writes
+//     them straight into TMEM (tcgen05.st, 16x256b shape) as the MMA's A
+//     operand; threads < 4*nshell
 //     write the B operand (the shells' hi and lo parts) to shared memory in
 //     the UMMA K-major core-matrix layout.  Then `full[stage]` and
 //     `fempty[buffer]` are signalled (one arrival per warp).
@@ -616,14 +617,17 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
 }
 
 // ---------------------------------------------------------------------------
-// host planning.  Pairs (i, j) = the two largest shell slots of each
-// triangle, column = the smallest.  The pairs of each shell i are cut into
-// runs of four consecutive shells j (a "slot": rows (i, J + y), y = 0..3, some
-// of them padding); two slots with the same run J make one producer row
-// thread (its loads of F_J .. F_J+3 serve both).  Row threads are sorted by
-// J so each tile's columns stay short, and the two threads that share a
-// quarter-warp load phase are matched to keep their shared-memory reads in
-// different banks.  Plans are cached per triangle list.
+// host planning, two kinds of plan (cached per triangle list):
+//  - runs: pairs (i, j) = the two largest shell slots of each triangle,
+//    column = the smallest.  The pairs of each shell i are cut into runs of
+//    four consecutive shells j (a "slot": rows (i, J + y), y = 0..3, some of
+//    them padding); two slots with the same run J make one producer row
+//    thread (its loads of F_J .. F_J+3 serve both).  Row threads are sorted by
+//    J so each tile's columns stay short, and the two threads that share a
+//    quarter-warp load phase are matched to keep their shared-memory reads in
+//    different banks.
+//  - cover (build_cover_plan): any shell pairs that meet every triangle, in
+//    blocks shaped like the row threads, where that needs fewer tiles.
 // ---------------------------------------------------------------------------
 struct HostPlan {
     Params base;           // pointers filled at launch
