@@ -701,9 +701,10 @@ static void finish_plan(HostPlan* hp, int ngroups, int maxslots, const std::vect
 // threads: up to 32 "two-slot" blocks {f1, f2} x {g0..g3} (tiles 0 and 1,
 // one load of each g serves both slots) chosen greedily by triangles newly
 // covered, then up to 32 "one-slot" blocks {f} x {g0..g3} (tile 2).  When
-// they cover every triangle the contraction runs on 3 tiles instead of 4:
-// 12 MMAs per chunk instead of 16 (Nmax 40: 32 + 29 blocks, 372 rows, against
-// 440 pairs + padding).  Returns false (and leaves hp untouched) otherwise.
+// they cover every triangle the contraction runs on 3 tiles (2 when no
+// one-slot block is needed) instead of 4: 12 (8) MMAs per chunk instead of
+// 16 (Nmax 40: 32 + 29 blocks, 372 rows, against 440 pairs + padding).
+// Returns false otherwise (the run plan then rebuilds hp).
 static bool build_cover_plan(HostPlan* hp, int nshell, const int32_t* tri_host, int ntri, int budget, size_t fixed) {
     const int S = nshell, T = ntri, W = (T + 63) / 64;
     std::vector<std::array<int, 3>> tri(T);
@@ -810,7 +811,46 @@ static bool build_cover_plan(HostPlan* hp, int nshell, const int32_t* tri_host, 
         blocks1.push_back(bb);
         for (int w = 0; w < W; ++w) unc[w] &= ~best_m[w];
     }
-    if (remaining() || blocks1.empty()) return false;   // no cover, or no gain over 2 tiles of runs
+    if (remaining()) return false;
+    const int ntiles = blocks1.empty() ? 2 : 3;           // two-slot blocks alone: tiles 0 and 1
+    // blocks at positions 2p and 2p + 1 of a lane quarter share quarter-warp
+    // load phases: pair them greedily by bank clashes (two field rows clash
+    // when they differ and bit 2 of their index agrees: same half of the
+    // swizzled row), trying every order of the partner's four g
+    auto clash = [](int r, int t) { return r != t && ((r >> 2) & 1) == ((t >> 2) & 1); };
+    auto pair_blocks = [&](std::vector<Block>& bl) {
+        std::vector<Block> out;
+        std::vector<bool> used(bl.size(), false);
+        for (size_t a = 0; a < bl.size(); ++a) {
+            if (used[a]) continue;
+            used[a] = true;
+            out.push_back(bl[a]);
+            int best = -1, bc = 1 << 30;
+            Block bb = bl[a];
+            for (size_t b = a + 1; b < bl.size(); ++b) {
+                if (used[b]) continue;
+                int gp[4] = {0, 1, 2, 3};
+                do {
+                    int c = 0;
+                    for (int k = 0; k < bl[a].nf; ++k) c += clash(bl[a].f[k], bl[b].f[k]);
+                    for (int y = 0; y < 4; ++y) c += clash(bl[a].g[y], bl[b].g[gp[y]]);
+                    if (c < bc) {
+                        bc = c;
+                        best = (int)b;
+                        bb = bl[b];
+                        for (int y = 0; y < 4; ++y) bb.g[y] = bl[b].g[gp[y]];
+                    }
+                } while (std::next_permutation(gp, gp + 4));
+            }
+            if (best >= 0) {
+                used[best] = true;
+                out.push_back(bb);
+            }
+        }
+        bl = out;
+    };
+    pair_blocks(blocks2);
+    pair_blocks(blocks1);
     // rows: two-slot block k at (q, x) = (k / 8, k % 8) in tiles 0 and 1,
     // one-slot block k at the same positions of tile 2; row (f, g_y) at lane 32q + x + 8y
     struct Row { int f, g; std::vector<std::pair<int, int>> cols; };   // (column, triangle)
@@ -843,7 +883,7 @@ static bool build_cover_plan(HostPlan* hp, int nshell, const int32_t* tri_host, 
     P.ngroups = 1;
     P.nshell = nshell;
     P.ntri = ntri;
-    G.ntiles = 3;
+    G.ntiles = ntiles;
     G.rows = 128 * G.ntiles;
     G.table_off = 0;
     hp->pair_row.assign((size_t)MAXROWS * 4, (int16_t)0);

@@ -28,12 +28,17 @@ def test_reference_loop_plans(nmax):
 
 def test_bench_workload_gets_three_tiles():
     """Nmax 40 (6350 triangles): 372 rows of a pair cover fit 3 tiles, so
-    12 MMAs per 32 voxels instead of 16 (440 (largest, middle) pairs need 4)."""
+    12 MMAs per 32 voxels instead of 16 (440 (largest, middle) pairs need 4);
+    Nmax 30 fits 2."""
     info = plan_check(40, core.triangles(1, 40) - 1)
     assert info == {"groups": 1, "tiles": 3, "cover": 1, "mma": 12, "slots": info["slots"], "wide": 1,
                     "macs": 3 * 128 * 2 * 2 * 40}
+    # Nmax 30: 38 row threads of runs need 4 tiles; 32 two-slot cover blocks fit 2
     info30 = plan_check(30, core.triangles(1, 30) - 1)
-    assert info30["cover"] == 0 and info30["tiles"] == 4
+    assert info30["cover"] == 1 and info30["tiles"] == 2 and info30["mma"] == 8
+    # Nmax 20: runs already fit 2 tiles, no cover is searched
+    info20 = plan_check(20, core.triangles(1, 20) - 1)
+    assert info20["cover"] == 0 and info20["tiles"] == 2
 
 
 @pytest.mark.parametrize("seed", [0, 1, 2])
