@@ -182,7 +182,8 @@ int pyspec_bk_contract(const float *fields, int ngrid, int nshell, const int32_t
  * of group 0, [2] 1 if the rows are a pair cover (0: runs of the triangles'
  * two largest shells), [3] MMAs per 32 voxels summed over groups, [4] Kahan
  * slots of group 0, [5] 1 if group 0 uses the wide MMA form, [6] tensor-core
- * multiply-adds per voxel summed over groups (the executed work).
+ * multiply-adds per voxel summed over groups (the executed work), [7] shared-
+ * memory bank clashes between the producer threads that share load phases.
  * Returns 0; PYSPEC_E_INVALID / PYSPEC_E_UNSUPPORTED where the contraction
  * would; PYSPEC_E_INVALID with a message if the plan fails the check.
  * ---------------------------------------------------------------------- */

@@ -1326,7 +1326,22 @@ extern "C" int pyspec_bk_plan_check(int nshell, const int32_t* tri_host, int ntr
         // tensor MACs per voxel: per tile M = 128 rows x (2 MMAs x 2N columns, or 3 x N)
         for (int t = 0; t < G.ntiles; ++t) macs += 128 * (G.wide ? 2 * 2 * G.tile_n[t] : 3 * G.tile_n[t]);
     }
-    const int64_t vals[7] = {P.ngroups, P.g[0].ntiles, hp->cover ? 1 : 0, mma, P.g[0].nslots, P.g[0].wide, macs};
-    for (int k = 0; k < ninfo && k < 7; ++k) info[k] = vals[k];
+    // shared-memory bank clashes between the row threads that share a
+    // quarter-warp load phase (entries 2p, 2p + 1): their F_i0, F_i1 and the
+    // four g loads (and the second slot's g where it has its own)
+    int64_t clashes = 0;
+    auto clash = [](int r, int t) { return r != t && ((r >> 2) & 1) == ((t >> 2) & 1); };
+    for (int g = 0; g < P.ngroups; ++g)
+        for (int e = 0; e < RT_PER_GROUP; e += 2) {
+            const int32_t* a = &hp->rt_tab[((size_t)g * RT_PER_GROUP + e) * RT_WORDS];
+            const int32_t* b = a + RT_WORDS;
+            for (int k = 0; k < 2; ++k) clashes += clash((a[0] >> (8 * k)) & 0xff, (b[0] >> (8 * k)) & 0xff);
+            for (int y = 0; y < 4; ++y) clashes += clash((a[1] >> (8 * y)) & 0xff, (b[1] >> (8 * y)) & 0xff);
+            if (a[2] != a[1] || b[2] != b[1])
+                for (int y = 0; y < 4; ++y) clashes += clash((a[2] >> (8 * y)) & 0xff, (b[2] >> (8 * y)) & 0xff);
+        }
+    const int64_t vals[8] = {P.ngroups, P.g[0].ntiles, hp->cover ? 1 : 0, mma, P.g[0].nslots, P.g[0].wide, macs,
+                             clashes};
+    for (int k = 0; k < ninfo && k < 8; ++k) info[k] = vals[k];
     return PYSPEC_OK;
 }
