@@ -1069,21 +1069,47 @@ static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri) {
                 }
                 if (best >= 0) { used[best] = true; order.push_back(best); }
             }
+            // the rows of a slot may sit in any order: the second thread of a
+            // load-phase pair takes the order of its runs that clashes least
+            // with its partner's loads
+            auto clash = [](int a, int b) { return a != b && ((a >> 2) & 1) == ((b >> 2) & 1); };
+            int prev_g[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
             for (size_t pos = 0; pos < order.size(); ++pos) {
                 const RowThread& r = blk[order[pos]];
                 const int q = (int)pos / 8, x = (int)pos % 8;
+                int gy[2][4];
+                for (int u = 0; u < 2; ++u)
+                    for (int y = 0; y < 4; ++y) gy[u][y] = std::min(r.s[u].J + y, nshell - 1);
+                int perm[4] = {0, 1, 2, 3};
+                if (pos & 1) {
+                    int gp[4] = {0, 1, 2, 3}, bc = 1 << 30;
+                    const bool two = r.s[1].J != r.s[0].J;
+                    do {
+                        int c = 0;
+                        for (int y = 0; y < 4; ++y) {
+                            c += clash(prev_g[0][y], gy[0][gp[y]]);
+                            if (two) c += clash(prev_g[1][y], gy[1][gp[y]]);
+                        }
+                        if (c < bc) {
+                            bc = c;
+                            for (int y = 0; y < 4; ++y) perm[y] = gp[y];
+                        }
+                    } while (std::next_permutation(gp, gp + 4));
+                }
+                for (int u = 0; u < 2; ++u)
+                    for (int y = 0; y < 4; ++y) prev_g[u][y] = gy[u][perm[y]];
                 int32_t* w = &hp->rt_tab[((size_t)g * RT_PER_GROUP + 32 * tp + pos) * RT_WORDS];
                 w[0] = (int32_t)((uint32_t)r.s[0].i | (uint32_t)r.s[1].i << 8);
                 for (int u = 0; u < 2; ++u) {
                     uint32_t gs = 0;
-                    for (int y = 0; y < 4; ++y) gs |= (uint32_t)std::min(r.s[u].J + y, nshell - 1) << (8 * y);
+                    for (int y = 0; y < 4; ++y) gs |= (uint32_t)gy[u][perm[y]] << (8 * y);
                     w[1 + u] = (int32_t)gs;
                 }
                 for (int u = 0; u < 2; ++u) {
                     const int tile = 2 * tp + u;
                     for (int y = 0; y < 4; ++y) {
-                        if (!(r.s[u].mask >> y & 1)) continue;
-                        const int i = r.s[u].i, j = r.s[u].J + y;
+                        if (!(r.s[u].mask >> perm[y] & 1)) continue;
+                        const int i = r.s[u].i, j = r.s[u].J + perm[y];
                         const auto& m = pairs[{i, j}];
                         const int lmin = m.begin()->first, lmax = m.rbegin()->first;
                         const int row = 128 * tile + 32 * q + x + 8 * y;
