@@ -43,6 +43,25 @@ SMALL_WORKLOAD = {"workload": "zeldovich-300k-192-step3-nmax40 (profiling case)"
 L2_FLUSH_BYTES = 512 << 20   # > 129 MB L2, written between timed steps
 
 
+def max_over_ranks(x, device=None):
+    """The slowest rank's value of x (max over the ranks of the process group);
+    x itself when no group of more than one rank is running.  device: where
+    the reduction tensor lives (cuda for NCCL, cpu for gloo)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1):
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world, units_per_rank, seconds_max):
+    """Whole-job throughput of `world` independent replicas: the units all
+    ranks processed over the slowest rank's time."""
+    return world * units_per_rank / seconds_max
+
+
 def plan_macs_per_voxel(nmax, ncut, step):
     """Tensor-core multiply-adds per voxel of the contraction plan for the
     triangle loop (host-side plan query of the library)."""
@@ -325,12 +344,8 @@ def run_gpu(args, rank, world, local_rank):
         stage = {name: float(np.mean([e[a].elapsed_time(e[b]) for e in evs]))
                  for name, a, b in (("fft_periodic", 0, 1), ("shell_fields", 1, 2), ("contraction", 2, 3),
                                     ("normalize", 3, 4))}
-        ms = float(np.sum(tot))
-        if world > 1:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        results[method] = {"ms_per_step": ms / steps, "bk_evals_per_s": world * steps / (ms / 1e3),
+        ms = max_over_ranks(float(np.sum(tot)), dev)
+        results[method] = {"ms_per_step": ms / steps, "bk_evals_per_s": job_rate(world, steps, ms / 1e3),
                            "triangles_per_s": plan.T / (stage["contraction"] / 1e3), "stage_ms": stage,
                            "gpu_launches": launches, "steps": steps, "clocks": clk.summary()}
         if method == "bf16x3":
@@ -384,11 +399,7 @@ def run_gpu(args, rank, world, local_rank):
         out = P.Bk_periodic(xyz_pinned, Lbox=L, Ngrid=n, step=step, Ncut=ncut, Nmax=nmax, method="bf16x3",
                             device=dev)
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dev)
     h2d = xyz_np.nbytes
     d2h = 7 * plans["bf16x3"].T * 8
 
@@ -430,7 +441,7 @@ def run_gpu(args, rank, world, local_rank):
             "bf16x3_vs_fp32_rel": {"median": float(np.median(rel)), "p99": float(np.percentile(rel, 99)),
                                    "max": float(rel.max())},
             "roofline": roofline, "cpu_baseline": cpu,
-            "e2e": {"value": world * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+            "e2e": {"value": job_rate(world, e2e_steps, e2e_s), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "api": "pyspectrum_gb300.pyspectrum.Bk_periodic(pinned xyz)"},
             "gpu_launches": main["gpu_launches"], "clocks": main["clocks"], "fft3d_comparator": fftcmp}
     print(json.dumps(line), flush=True)
