@@ -102,6 +102,25 @@ def test_arbitrary_triangle_lists():
         assert (np.abs(got - ref) / mag).max() < tol, method
 
 
+def test_cover_plan_narrow_three_tiles():
+    """The Nmax 40 loop moved to shells 7..46 of 48: its pair cover still fits
+    3 tiles, but columns up to 46 exceed the wide form's TMEM budget, so the
+    3-tile narrow form (three MMAs per tile and k-step) runs."""
+    n, step, nmax, jmin = 64, 1, 48, 1
+    fields = _fields(n, step, jmin, nmax, seed=11)
+    slots = np.ascontiguousarray(core.triangles(1, 40) - 1 + 7, dtype=np.int32)
+    info = np.zeros(8, dtype=np.int64)
+    call("pyspec_bk_plan_check", nmax, slots.ctypes.data_as(ctypes.c_void_p), slots.shape[1],
+         info.ctypes.data_as(ctypes.c_void_p), 8)
+    assert info[1] == 3 and info[2] == 1 and info[5] == 0   # 3 tiles, pair cover, narrow form
+    ref, mag = _reference(fields, slots)
+    mag = np.maximum(mag, 1e-300)
+    got, status = _contract(fields, n, slots, 1)
+    assert status == 0
+    err = np.abs(got - ref) / mag
+    assert err.max() < 3e-5 and np.median(err) < 3e-6
+
+
 @pytest.mark.parametrize("method", [0, 1])
 def test_repeated_triangle_rejected(method):
     n = 16
