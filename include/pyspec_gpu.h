@@ -205,7 +205,11 @@ int pyspec_bk_plan_check(int nshell, const int32_t *tri_host, int ntri, int64_t 
  *  - All calls share the one array: calls whose work overlaps on the GPU race
  *    and must be ordered by the caller.
  *  - The first call on a device looks up the array's address with that
- *    device current; make it before any stream capture.
+ *    device current, and the first call with a given triangle list builds
+ *    its tile plan in page-locked host memory.  Neither may happen inside a
+ *    stream capture: a call on a capturing stream returns PYSPEC_E_INVALID
+ *    (and leaves the capture intact) unless an earlier call, outside any
+ *    capture, used the same device and the same triangle list.
  * ---------------------------------------------------------------------- */
 #define PYSPEC_NOALLOC_SCRATCH_BYTES (16u << 20)
 int pyspec_bk_contract_noalloc(const float *fields, int ngrid, int nshell,

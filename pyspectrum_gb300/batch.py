@@ -124,12 +124,18 @@ class BkBatch:
             geo.plan.normalize(True, nbar, kf)
             host = torch.empty(geo.plan.out.shape, dtype=torch.float64, pin_memory=True)
             host.copy_(geo.plan.out, non_blocking=True)
+            status = None
+            if self.method == "bf16x3":     # the contraction's status word of this mock
+                status = torch.empty(1, dtype=torch.int32, pin_memory=True)
+                status.copy_(geo.plan.status_word(), non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(cur)
-            staged.append((ev, host, geo, n, npart, nbar))
+            staged.append((ev, host, status, geo, n, npart, nbar))
         results = []
-        for ev, host, geo, n, npart, nbar in staged:
+        for ev, host, status, geo, n, npart, nbar in staged:
             ev.synchronize()
+            if status is not None:
+                core.check_contract_status(int(status[0]))
             results.append(_result_dict(geo.plan, host.numpy(), L, n, self.step, self.ncut, self.nmax, npart,
                                         nbar, kf))
         return results

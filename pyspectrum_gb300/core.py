@@ -258,10 +258,18 @@ class BkPlan:
         self.normalize(apply_units, nbar, kf)
         return self.out
 
+    def status_word(self) -> torch.Tensor:
+        """The contraction's int32 status word on the device (tensor-core
+        method: 0, or the code of a bounded wait that timed out)."""
+        return self.ws_con[:4].view(torch.int32)
+
     def result(self, apply_units=False):
         """Copy the normalised arrays to the host as the reference's output dict.
-        Only triangles with counts > 0 are returned (all arrays aligned)."""
+        Only triangles with counts > 0 are returned (all arrays aligned).
+        Raises ContractTimeout if the tensor-core contraction stopped early."""
         out = self.out.cpu().numpy()
+        if self.method == "bf16x3":
+            check_contract_status(self.status_word().item())
         keep = self.counts_np > 0
         tri = self.tri_np[:, keep]
         res = {
@@ -277,6 +285,25 @@ class BkPlan:
 
 
 _plans: dict = {}
+
+# Codes the tensor-core contraction leaves in the int32 at workspace offset 0
+# when one of its bounded waits gives up (the kernel then stops early and its
+# sums are incomplete).
+CONTRACT_STATUS = {1: "producer wait for a field copy or a free stage", 2: "accumulator drain",
+                   3: "MMA wait for the operands", 4: "MMA wait for the drain", 5: "copy wait for a free buffer"}
+
+
+class ContractTimeout(RuntimeError):
+    """A bounded wait inside the tensor-core contraction timed out."""
+
+
+def check_contract_status(word: int) -> None:
+    """Raise ContractTimeout if the contraction's status word is not 0."""
+    word = int(word)
+    if word != 0:
+        what = CONTRACT_STATUS.get(word, "unknown wait")
+        raise ContractTimeout(f"tensor-core contraction stopped early (status {word}: {what} timed out); "
+                              "its triangle sums are incomplete")
 
 
 def get_plan(Ngrid, step, Ncut, Nmax, method="fp32", device=None) -> BkPlan:

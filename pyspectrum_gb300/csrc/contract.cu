@@ -348,11 +348,47 @@ static void grid_dims(int64_t nvox, int ntile, int* gx, int* gy, int* per) {
     *gx = (int)std::max<int64_t>(1, std::min<int64_t>(nch, std::max(1, sms / *gy)));
 }
 
+// The cached plan of a list, or nullptr (never plans, never allocates).
+static HostPlan* find_plan(int nshell, const int32_t* tri_host, int ntri) {
+    std::vector<int32_t> key(tri_host, tri_host + 3 * (size_t)ntri);
+    key.push_back(nshell);
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_plans.find(key);
+    return it == g_plans.end() ? nullptr : it->second;
+}
+
 }  // namespace simt
 
+int contract_fp32_need(int64_t nvox, int nshell, const int32_t* tri_host, int ntri, bool may_plan, size_t* need) {
+    using namespace simt;
+    HostPlan* hp = may_plan ? plan(nshell, tri_host, ntri) : find_plan(nshell, tri_host, ntri);
+    if (hp == nullptr) {
+        set_error("this triangle list has no plan yet and planning allocates page-locked host memory, which a "
+                  "stream capture forbids: make one call with this list outside the capture first");
+        return PYSPEC_E_INVALID;
+    }
+    if (!hp->ok) {
+        set_error("the triangle list repeats a triangle");
+        return PYSPEC_E_INVALID;
+    }
+    if (!may_plan && hp->image_src == hp->image.data()) {
+        set_error("the tile tables of this list are in pageable host memory (page-locked allocation failed), "
+                  "which a captured copy cannot read");
+        return PYSPEC_E_INVALID;
+    }
+    int gx, gy, per;
+    grid_dims(nvox, hp->ntile, &gx, &gy, &per);
+    *need = hp->image.size() + al((size_t)gx * ntri * sizeof(double));
+    return PYSPEC_OK;
+}
+
 size_t contract_fp32_ws(int64_t nvox, int nshell, int ntri) {
-    // worst-case tile count: one tile per (pair row, l group) with all pairs distinct
-    const size_t maxtile = (size_t)std::max(1, ntri);
+    // worst-case tile count: plan() emits, for each group of MT pair rows, one
+    // tile per NT-wide window of l from the group's lowest to its highest l,
+    // empty windows included; a list has at most ntri distinct pairs
+    const size_t groups = ((size_t)std::max(1, ntri) + simt::MT - 1) / simt::MT;
+    const size_t windows = ((size_t)std::max(1, nshell) + simt::NT - 1) / simt::NT;
+    const size_t maxtile = groups * windows;
     const size_t tables = simt::al(maxtile * 16) + simt::al(maxtile * 2) + simt::al(maxtile * 128);
     int sms = 152, dev = 0;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -13,6 +13,10 @@ int contract_simple_impl(const T* fields, int64_t fstride, int nshell, const int
 size_t contract_fp32_ws(int64_t nvox, int nshell, int ntri);
 int contract_fp32_impl(const float* fields, int64_t nvox, int nshell, const int32_t* tri_host, int ntri,
                        double* bsum, void* ws, size_t ws_bytes, cudaStream_t st);
+// Exact scratch bytes contract_fp32_impl uses for this list.  may_plan=false
+// only consults the plan cache (no host allocation) and fails if the list has
+// no cached plan or its tables are not page-locked.
+int contract_fp32_need(int64_t nvox, int nshell, const int32_t* tri_host, int ntri, bool may_plan, size_t* need);
 
 // tcgen05 split-BF16 contraction (contract_tc.cu)
 size_t contract_tc_ws(int64_t nvox, int nshell, int ntri);

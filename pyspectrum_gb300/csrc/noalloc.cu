@@ -14,8 +14,12 @@
 // sums it uses before the kernel runs.  All calls share the one array, so two
 // calls whose work overlaps on the GPU (different streams, or different host
 // threads without ordering) race; callers order them.  The first call on a
-// device looks the array's device address up with that device current; make
-// that first call before any stream capture.
+// device looks the array's device address up with that device current, and
+// the first call with a given triangle list builds that list's tile plan in
+// page-locked host memory; both are forbidden inside a stream capture, so a
+// call made while its stream is capturing fails with PYSPEC_E_INVALID unless
+// an earlier call on that device with that list, outside any capture, has
+// done them.
 #include <mutex>
 #include "common.cuh"
 #include "contract.cuh"
@@ -27,8 +31,9 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[PYSPEC_NOALLOC_
 static std::mutex g_noalloc_mu;
 static void* g_noalloc_addr[256] = {nullptr};
 
-// Device address of the array on the current device (looked up once per device).
-static int noalloc_scratch(void** out) {
+// Device address of the array on the current device (looked up once per
+// device; while capturing, only an address looked up before is returned).
+static int noalloc_scratch(void** out, bool capturing) {
     int dev = 0;
     PYSPEC_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 256) {
@@ -37,6 +42,11 @@ static int noalloc_scratch(void** out) {
     }
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
     if (g_noalloc_addr[dev] == nullptr) {
+        if (capturing) {
+            set_error("the first no-alloc call on device %d runs inside a stream capture; make one call on this "
+                      "device outside the capture first", dev);
+            return PYSPEC_E_INVALID;
+        }
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || p == nullptr) {
@@ -60,14 +70,20 @@ extern "C" int pyspec_bk_contract_noalloc(const float* fields, int ngrid, int ns
                      "bad arguments");
     if (ntri == 0) return PYSPEC_OK;
     const int64_t V = (int64_t)ngrid * ngrid * ngrid;
-    const size_t need = contract_fp32_ws(V, nshell, ntri);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    PYSPEC_CUDA(cudaStreamIsCapturing(as_stream(stream), &cap));
+    const bool capturing = cap != cudaStreamCaptureStatusNone;
+    // the scratch this list needs, from its tile plan (planned here unless the
+    // stream is capturing, where only an existing plan may be used)
+    size_t need = 0;
+    PYSPEC_TRY(contract_fp32_need(V, nshell, tri_host, ntri, !capturing, &need));
     if (need > (size_t)PYSPEC_NOALLOC_SCRATCH_BYTES) {
         set_error("this contraction needs %zu bytes of scratch; the fixed scratch array holds %zu "
                   "(use pyspec_bk_contract with a workspace)", need, (size_t)PYSPEC_NOALLOC_SCRATCH_BYTES);
         return PYSPEC_E_INVALID;
     }
     void* scratch = nullptr;
-    PYSPEC_TRY(noalloc_scratch(&scratch));
+    PYSPEC_TRY(noalloc_scratch(&scratch, capturing));
     return contract_fp32_impl(fields, V, nshell, tri_host, ntri, bsum, scratch, PYSPEC_NOALLOC_SCRATCH_BYTES,
                               as_stream(stream));
 }

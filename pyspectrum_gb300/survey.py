@@ -75,6 +75,8 @@ def _b0_from_half(half, alpha, I12, I13, I22, I23, I33, Nmax, Ncut, step, method
     plan.shells(half)
     plan.contract()
     bsum = plan.bsum.cpu().numpy()
+    if plan.method == "bf16x3":
+        core.check_contract_status(plan.status_word().item())
     p0sum = plan.p0sum.cpu().numpy()
     V = float(n) ** 3
     jmin = plan.jmin
