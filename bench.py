@@ -10,8 +10,11 @@ PCS+interlaced assignment -> 3D FFT -> interlacing combine -> 40 shell fields
 contraction and the inputs resident in HBM; the plain FP32 CUDA-core form is
 timed on the same inputs and reported under "methods".  `e2e` times the public
 API (pyspectrum_gb300.pyspectrum.Bk_periodic) from pinned host positions to
-the host result dictionary.  `cpu_baseline` times the CPU restatement of the
-reference on a bounded sample of the same workload (see --impl reference).
+the host result dictionary.  `cpu_baseline` times one full evaluation of the
+same workload by the all-core C/OpenMP restatement of the reference's CPU
+path (oracle/cpu_ref.py); `--impl reference` times full evaluations of it
+(no extrapolation) and loads no library of this package.  `fp64_error` gives
+both contraction forms' error against float64 sums over all triangles.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 Under torchrun (N > 1) every rank runs an independent replica ("replicas
@@ -41,6 +44,14 @@ SMALL_WORKLOAD = {"workload": "zeldovich-300k-192-step3-nmax40 (profiling case)"
                   "Lbox": 1500.0, "Ngrid": 192, "step": 3, "Ncut": 3, "Nmax": 40, "triangles": 6350, "shells": 40,
                   "field": "GRF P(k)~k^-1.5 on 192^3, rms displacement 5 Mpc/h", "seed": 2}
 L2_FLUSH_BYTES = 512 << 20   # > 129 MB L2, written between timed steps
+DATA = "synthetic (seeded Zel'dovich mock)"
+
+
+def bench_config():
+    """The workload description both arms print (the same dict on both)."""
+    W = WORKLOAD
+    gb = W["shells"] * W["Ngrid"] ** 3 * 4 / 1e9
+    return dict(W, l2=f"device arm: L2 flushed between steps (512 MB write); {gb:.1f} GB of shell fields per step")
 
 
 def max_over_ranks(x, device=None):
@@ -83,86 +94,120 @@ def _peaks():
 
 
 # ---------------------------------------------------------------------------
-# CPU reference arm: the oracle port of the reference's CPU path, timed on a
-# bounded sample of the same workload and extrapolated to one Bk evaluation.
+# Workload generator (numpy/scipy only, shared by both arms)
 # ---------------------------------------------------------------------------
-def cpu_reference_sample(xyz_np, n_shell_sample=4, n_tri_sample=24):
-    """Reference-structured CPU pipeline (pyspectrum.py:285-457 with the
-    Fortran parts restated): assignment (C, one core), complex64 FFT (scipy,
-    all cores, like threaded FFTW), interlacing combine, reflection, then a
-    sample of shell FFTs and triangle einsums, extrapolated to 40 shells and
-    6350 triangles.  Returns (seconds per Bk evaluation, details)."""
+def zeldovich_positions(npart, Lbox, ngrid, seed, slope=-1.5, rms_disp=5.0):
+    """Seeded Zel'dovich box: a Gaussian random field with P(k) ~ k^slope on
+    an ngrid^3 grid (white noise from numpy's PCG64), its displacement
+    psi(k) = i k delta(k) / k^2 scaled to rms |psi| = rms_disp Mpc/h, applied
+    (nearest grid point) to a lattice of ceil(npart^(1/3))^3 cells with a
+    random offset inside each cell.  Returns float64 (3, npart) positions in
+    [0, Lbox).  numpy/scipy only, so the reference arm loads no library of
+    this package; the device arm uses the same particles."""
     import scipy.fft as sfft
-    from oracle import pyspec_oracle as O
-    cores = os.cpu_count() or 1
+    n = int(ngrid)
+    rng = np.random.default_rng(seed)
+    g = sfft.fftn(rng.standard_normal((n, n, n), dtype=np.float32).astype(np.complex128), workers=-1)
+    k = np.fft.fftfreq(n, d=1.0 / n)
+    kz, ky, kx = k.reshape(n, 1, 1), k.reshape(1, n, 1), k.reshape(1, 1, n)
+    k2 = kx * kx + ky * ky + kz * kz
+    k2[0, 0, 0] = 1.0
+    amp = k2 ** (slope / 4.0)
+    amp[0, 0, 0] = 0.0
+    g *= amp
+    psi = np.empty((3, n, n, n), dtype=np.float32)
+    for d, kd in enumerate((kx, ky, kz)):
+        psi[d] = sfft.ifftn(g * (1j * kd / k2), workers=-1).real * float(n) ** 3
+    del g
+    psi *= np.float32(rms_disp / np.sqrt((psi.astype(np.float64) ** 2).sum(0).mean()))
+    npart = int(npart)
+    m = int(round(npart ** (1.0 / 3.0)))
+    if m ** 3 < npart:
+        m += 1
+    rng = np.random.default_rng(seed + 1000)
+    cells = np.arange(m ** 3) if m ** 3 == npart else np.sort(rng.choice(m ** 3, size=npart, replace=False))
+    iz, rem = np.divmod(cells, m * m)
+    iy, ix = np.divmod(rem, m)
+    q = (np.stack([ix, iy, iz]).astype(np.float64) + rng.uniform(0.0, 1.0, size=(3, npart))) * (Lbox / m)
+    idx = np.clip((q / Lbox * n).astype(np.int64), 0, n - 1)
+    disp = psi[:, idx[2], idx[1], idx[0]].astype(np.float64)
+    return np.mod(q + disp, Lbox)
+
+
+def make_positions_np(seed=None):
     W = WORKLOAD
-    n, L, step = W["Ngrid"], W["Lbox"], W["step"]
-    t0 = time.perf_counter()
-    xyzs = O.clip_positions(xyz_np, L)
-    g = O.assign_quad(xyzs, np.ones(xyz_np.shape[1], np.float32), np.float32(n / L), 0.0, n)
-    t_assign = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    G = sfft.ifftn(g.astype(np.complex64), workers=cores) * np.float32(n ** 3)
-    t_fft = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    half = O.fcomb_periodic(G, float(xyz_np.shape[1]))
-    full = O.reflect_delta(half, n).astype(np.complex64)
-    t_fcomb = time.perf_counter() - t0
-    del g, G
-    irk = O.shell_index(n, step)
-    shells = {}
-    t0 = time.perf_counter()
-    for j in range(1, n_shell_sample + 1):
-        tmp = np.where(irk == j, full, np.complex64(0))
-        F = np.real(sfft.fftn(tmp, workers=cores)).astype(np.float64)
-        _ = np.einsum("i,i", F.ravel(), F.ravel())
-        shells[j] = F
-    t_shell = (time.perf_counter() - t0) / n_shell_sample
-    tri = [(i, j, l) for i in range(1, 5) for j in range(1, i + 1) for l in range(max(i - j, 1), j + 1)]
-    tri = (tri * ((n_tri_sample // len(tri)) + 1))[:n_tri_sample]
-    t0 = time.perf_counter()
-    for i, j, l in tri:
-        _ = np.einsum("i,i,i", shells[i].ravel(), shells[j].ravel(), shells[l].ravel())
-    t_tri = (time.perf_counter() - t0) / n_tri_sample
-    total = t_assign + t_fft + t_fcomb + W["shells"] * t_shell + W["triangles"] * t_tri
-    det = {"assign_s": t_assign, "fft_s": t_fft, "fcomb_reflect_s": t_fcomb, "per_shell_s": t_shell,
-           "per_triangle_s": t_tri, "extrapolated_s_per_eval": total}
-    sample = (f"full FFT_periodic (1M particles, 360^3) + {n_shell_sample} of 40 shell FFTs + {n_tri_sample} of "
-              f"6350 triangle einsums, extrapolated; FFTs on {cores} threads, assignment and einsums on 1 "
-              f"thread as in the reference")
-    return total, det, sample, cores
+    return zeldovich_positions(W["npart"], W["Lbox"], W["Ngrid"], W["seed"] if seed is None else seed)
 
 
-def make_positions_np(seed):
-    """Same particles as the GPU arm, generated on the GPU when available."""
+def reference_counts():
+    """Exact triangle counts of the workload's geometry, read the way the
+    reference reads its count cache (pyspectrum.py:407, 962-973): from the
+    reference's own shipped cache for Ngrid 360 / Nmax 40 / Ncut 3 / step 3
+    (stored in tests/golden as integers); other geometries (the profiling
+    case) are counted by the oracle's float64 shell-indicator sums."""
+    W = WORKLOAD
+    if (W["Ngrid"], W["Nmax"], W["Ncut"], W["step"]) == (360, 40, 3, 3):
+        return np.load(os.path.join(ROOT, "tests", "golden", "counts_ref360.npz"))["nmax40"]
     import torch
-    from pyspectrum_gb300 import mocks
+    from oracle import torch_fp64 as TF
+    from oracle import cpu_ref
+    n, step, jmin, nmax = W["Ngrid"], W["step"], W["Ncut"] // W["step"], W["Nmax"]
+    tri, _ = cpu_ref.triangles(jmin, nmax)
+    I, _ = TF.shell_fields(torch.ones((n, n, n), dtype=torch.complex128), step, jmin, nmax)
+    craw, _ = TF.triangle_sums(I, tri - jmin, with_abs=False)
+    return np.rint(craw / float(n) ** 3).astype(np.int64)
+
+
+# ---------------------------------------------------------------------------
+# CPU reference arm: the all-core C restatement of the reference's CPU path
+# (oracle/cpu_ref.py), full Bk_periodic evaluations, no extrapolation.
+# ---------------------------------------------------------------------------
+def cpu_reference_eval(xyz_np, counts):
+    """One full Bk_periodic evaluation of the workload on all host cores
+    (pyspectrum.py:285-457 structure: float32 grid, complex64 FFTs, one full
+    3D FFT per shell, float64 triangle sums).  Returns (seconds, stages)."""
+    from oracle import cpu_ref
     W = WORKLOAD
-    if torch.cuda.is_available():
-        x = mocks.zeldovich_mock(W["npart"], W["Lbox"], ngrid=W["Ngrid"], seed=seed)
-        return x, x.cpu().numpy()
-    raise RuntimeError("the workload generator runs on the GPU")
+    t0 = time.perf_counter()
+    _, stages = cpu_ref.bk_periodic_cpu(xyz_np, W["Lbox"], W["Ngrid"], W["step"], W["Ncut"], W["Nmax"], counts)
+    return time.perf_counter() - t0, stages
+
+
+def cpu_sample_text(cores):
+    W = WORKLOAD
+    return (f"full Bk_periodic evaluations ({W['npart']} particles, {W['Ngrid']}^3, {W['shells']} shells, "
+            f"{W['triangles']} triangles), no extrapolation: C/OpenMP assignment, fcomb and triangle sums, "
+            f"complex64 pocketfft FFTs, on {cores} host threads")
+
+
+REF_BUDGET_S = 150.0     # the reference arm times at most this much CPU work
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    import torch
-    _, xyz_np = make_positions_np(WORKLOAD["seed"])
-    torch.cuda.synchronize()
+    from oracle import cpu_ref
+    xyz_np = make_positions_np()
+    counts = reference_counts()
+    cores = cpu_ref.cores()
     per = []
-    det = sample = cores = None
-    for _ in range(max(1, args.steps)):
-        total, det, sample, cores = cpu_reference_sample(xyz_np)
-        per.append(total)
-    sec = float(np.mean(per))
-    value = 1.0 / sec
+    for _ in range(min(args.warmup, 1)):             # page-in, FFT plans, OpenMP pool
+        cpu_reference_eval(xyz_np, counts)
+    det = None
+    for k in range(max(1, args.steps)):
+        sec, det = cpu_reference_eval(xyz_np, counts)
+        per.append(sec)
+        if sum(per) + sec > REF_BUDGET_S:            # bounded: never run past the budget
+            break
+    total = float(np.sum(per))
+    value = len(per) / total
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64/c64 (CPU)", "data": "synthetic",
-            "config": WORKLOAD,
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
-                             "stages": det},
+            "steps": len(per), "steps_requested": args.steps, "warmup": min(args.warmup, 1),
+            "ms_per_step": total / len(per) * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 grid and FFTs, f64 sums (CPU)", "data": DATA,
+            "config": bench_config(),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": cpu_sample_text(cores), "stages_s": det},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -234,20 +279,16 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-FP64_SHELLS = (1, 2, 3, 5, 8, 13, 20, 27, 34, 40)
-
-
 def fp64_error(half, plans):
-    """Error of both contraction forms against float64 sums on the bench box:
-    the shell fields of FP64_SHELLS rebuilt from the same delta(k) with
-    complex128 FFTs (scipy, all host cores) and the triangles among those
-    shells summed in float64.  Reports, per form, the median and maximum
-    |dB/B|, the maximum over triangles with condition number
-    sum|F_iF_jF_l| / |sum F_iF_jF_l| < 1e3, and the maximum error normalised by
-    sum|F_iF_jF_l|."""
-    import scipy.fft as sfft
+    """Error of both contraction forms against float64 sums over ALL the
+    workload's triangles: the shell fields rebuilt from the same delta(k)
+    with complex128 FFTs and the triangle sums taken in float64
+    (oracle/torch_fp64.py, plain torch on the device).  Per form: median and
+    maximum |dB/B|, the maximum over triangles with condition number
+    sum|F_iF_jF_l| / |sum F_iF_jF_l| < 1e3, and the maximum error normalised
+    by sum|F_iF_jF_l|."""
     import torch
-    from pyspectrum_gb300 import core
+    from oracle import torch_fp64 as TF
     t0 = time.perf_counter()
     bsums = {}
     for name, pl in plans.items():          # both forms from this same delta(k)
@@ -255,31 +296,16 @@ def fp64_error(half, plans):
         pl.contract()
         bsums[name] = pl.bsum.cpu().numpy()
     plan = plans["bf16x3"]
-    n, step = plan.n, plan.step
-    delta = core.reflect_half(half).cpu().numpy().astype(np.complex128)
+    full = TF.reflect_half(half)
+    F, _ = TF.shell_fields(full, plan.step, plan.jmin, plan.nmax)
+    del full
+    exact, absum = TF.triangle_sums(F, plan.tri_np - plan.jmin)
+    del F
     torch.cuda.empty_cache()
-    a = np.minimum(np.arange(n), n - np.arange(n)).astype(np.int64)
-    d2 = a[:, None, None] ** 2 + a[None, :, None] ** 2 + a[None, None, :] ** 2
-    irk = np.floor(np.sqrt(d2.astype(np.float64)) / step + 0.5).astype(np.int64)
-    irk -= ((2 * irk - 1) ** 2 * step * step > 4 * d2) & (irk > 0)        # exact integer shell rule
-    irk += (2 * irk + 1) ** 2 * step * step <= 4 * d2
-    F = {j: np.real(sfft.fftn(np.where(irk == j, delta, 0), workers=-1)).ravel() for j in FP64_SHELLS}
-    del delta, irk, d2
-    loop = plan.tri_np
-    sel = [t for t in range(loop.shape[1]) if all(int(v) in F for v in loop[:, t])]
-    exact = np.empty(len(sel))
-    absum = np.empty(len(sel))
-    for k, t in enumerate(sel):
-        prod = F[int(loop[0, t])] * F[int(loop[1, t])] * F[int(loop[2, t])]
-        exact[k], absum[k] = prod.sum(), np.abs(prod).sum()
-    cond = absum / np.abs(exact)
-    out = {"triangles": len(sel), "shells": list(FP64_SHELLS), "seconds": time.perf_counter() - t0}
+    out = {"triangles": int(plan.T), "shells": f"{plan.jmin}..{plan.nmax}", "seconds": time.perf_counter() - t0,
+           "reference": "float64 fields (complex128 FFTs) and float64 sums from the same delta(k)"}
     for name, b in bsums.items():
-        err = np.abs(b[sel] - exact)
-        rel = err / np.abs(exact)
-        out[name] = {"median_rel": float(np.median(rel)), "max_rel": float(rel.max()),
-                     "max_rel_cond_lt_1e3": float(rel[cond < 1e3].max()),
-                     "normalised_max": float((err / absum).max())}
+        out[name] = TF.error_report(b, exact, absum)
     return out
 
 
@@ -292,7 +318,8 @@ def run_gpu(args, rank, world, local_rank):
     dev = torch.device("cuda", local_rank)
     W = WORKLOAD
     n, L, step, ncut, nmax = W["Ngrid"], W["Lbox"], W["step"], W["Ncut"], W["Nmax"]
-    x, xyz_np = make_positions_np(W["seed"])
+    xyz_np = make_positions_np()
+    x = torch.from_numpy(xyz_np).to(dev)
     npart = x.shape[1]
     nbar = npart / L ** 3
     kf = 2 * np.pi / L
@@ -425,14 +452,16 @@ def run_gpu(args, rank, world, local_rank):
                 "(1.133 GB read) scaled by the voxel count; equal to the algorithmic bytes (fields read once)"}
     cpu = None
     if not args.no_cpu_baseline:
-        total, det, sample, cores = cpu_reference_sample(xyz_np)
-        cpu = {"value": 1.0 / total, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
-               "stages": det}
+        from oracle import cpu_ref
+        cores = cpu_ref.cores()
+        sec, det = cpu_reference_eval(xyz_np, reference_counts())
+        cpu = {"value": 1.0 / sec, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": cpu_sample_text(cores).replace("evaluations", "evaluation (one)"), "stages_s": det}
     line = {"metric": METRIC, "value": main["bk_evals_per_s"], "unit": UNIT, "n_gpus": world,
             "steps": main["steps"], "warmup": args.warmup, "ms_per_step": main["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3 (f32 fields, f64 sums)",
-            "data": "synthetic (seeded Zel'dovich mock)",
-            "config": dict(WORKLOAD, l2="flushed between steps (512 MB write); inputs 7.5 GB of fields per step"),
+            "data": DATA,
+            "config": bench_config(),
             "triangles_per_s": main["triangles_per_s"],
             "methods": results,
             "tc_over_fp32": results["fp32"]["ms_per_step"] / main["ms_per_step"],
@@ -491,7 +520,7 @@ def run_profile_shells(jtop):
     from pyspectrum_gb300._lib import call, ptr, stream_ptr
     W = WORKLOAD
     n, L, step = W["Ngrid"], W["Lbox"], W["step"]
-    x, _ = make_positions_np(W["seed"])
+    x = torch.from_numpy(make_positions_np()).cuda()
     xyzs, ws = core.prepare_positions(x, L)
     half = core.fft_periodic_half(xyzs, ws, n, L, float(x.shape[1]))
     del x, xyzs, ws
@@ -518,7 +547,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-fp64-check", action="store_true", help="skip the float64 error check (about 30 s of CPU)")
+    ap.add_argument("--no-fp64-check", action="store_true", help="skip the float64 error check of all triangles")
     ap.add_argument("--small", action="store_true", help="run the 192^3 profiling case instead of the bench workload")
     ap.add_argument("--batch", action="store_true",
                     help="time 64 mixed-size mocks through Bk_periodic_batch instead of the bench workload")
@@ -538,10 +567,7 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
-        if rank == 0:
-            import torch
-            torch.cuda.set_device(local_rank)
-            run_reference(args, rank, world)
+        run_reference(args, rank, world)      # host cores only; other ranks exit without work
         return
     if world > 1:
         import torch.distributed as dist

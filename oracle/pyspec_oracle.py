@@ -40,8 +40,8 @@ Parity status of this oracle
 FFT convention: the reference calls FFTW 3.x single precision (version not
 pinned by the reference; ``setup.py`` mentions 3.3.4 and 3.3.8).  FFTW's
 published transforms are the plain DFTs; this oracle evaluates them in
-float64 with ``numpy.fft`` (``ifftn * N**3`` for FFTW_BACKWARD unnormalised,
-``fftn`` for FFTW_FORWARD).
+float64 with pocketfft (``scipy.fft``, numpy's FFT on all host cores:
+``ifftn * N**3`` for FFTW_BACKWARD unnormalised, ``fftn`` for FFTW_FORWARD).
 
 Array convention: every grid is indexed ``[x, y, z]`` as in the reference's
 numpy code; half grids are ``[0..N/2, y, z]``.
@@ -86,6 +86,13 @@ def _c():
 # --------------------------------------------------------------------------
 # a1 / a2 / a3 / a4 : particles -> half-complex delta(k)
 # --------------------------------------------------------------------------
+def _sfft():
+    """scipy.fft: numpy's pocketfft algorithm in double precision, on all
+    host cores."""
+    import scipy.fft
+    return scipy.fft
+
+
 def clip_positions(xyz, Lbox):
     """pyspectrum.py:938-941: clip to [0, L(1-1e-6)] in float64, store float32."""
     xyz = np.asarray(xyz)
@@ -112,7 +119,7 @@ def assign_quad(xyzs, w, kf_ks, offset, ngrid):
 def fft_backward(g):
     """pyspectrum.py:1072-1075: FFTW_BACKWARD, ``normalise_idft=False``."""
     n = g.shape[0]
-    return np.fft.ifftn(g) * float(n) ** 3
+    return _sfft().ifftn(g, workers=-1) * float(n) ** 3
 
 
 def _fcomb_tables(n):
@@ -271,7 +278,7 @@ def shell_fields(delta_full, step, jmin, nmax):
     p0k = np.zeros(nmax)
     for j in range(jmin, nmax + 1):
         tmp = np.where(irk == j, delta_full, 0)
-        F[j] = np.real(np.fft.fftn(tmp))
+        F[j] = np.real(_sfft().fftn(tmp, workers=-1))
         with np.errstate(invalid="ignore", divide="ignore"):
             p0k[j - 1] = np.sum(F[j] ** 2) / float(n) ** 3 / nk[j]
     return F, p0k, nk
@@ -286,7 +293,7 @@ def counts_Bk123(Ngrid, Nmax, Ncut, step):
     irk = shell_index(n, step)
     I = {}
     for j in range(jmin, Nmax + 1):
-        I[j] = np.real(np.fft.fftn((irk == j).astype(np.complex128)))
+        I[j] = np.real(_sfft().fftn((irk == j).astype(np.complex128), workers=-1))
     counts = np.zeros((Nmax, Nmax, Nmax))
     for i, j, l, _ in triangles(jmin, Nmax):
         counts[i - 1, j - 1, l - 1] = np.einsum("i,i,i", I[i].ravel(), I[j].ravel(), I[l].ravel())
