@@ -48,6 +48,10 @@ extern "C" {
 /* Contraction methods for pyspec_bk_contract. */
 #define PYSPEC_CONTRACT_FP32 0    /* FP32 CUDA-core, FP32 per-thread, FP64 across blocks */
 #define PYSPEC_CONTRACT_BF16X3 1  /* tcgen05 tensor cores, hi+lo BF16 split, 3 products */
+/* Flag OR-ed into the BF16X3 method: plan the tensor-core tiles from runs of
+ * each triangle's two largest shells even where a pair cover would need
+ * fewer tiles (same sums; for the autotuner, which times both plans). */
+#define PYSPEC_CONTRACT_RUN_PLAN 0x100
 
 int pyspec_abi_version(void);
 
@@ -85,6 +89,18 @@ int pyspec_prepare_positions(const double *xyz, int64_t dim_stride, const double
 int pyspec_assign_pcs_interlaced(const float *xyz, const float *w, int64_t np, int ngrid,
                                  float kf_ks, float offset, float *grid, void *stream);
 
+/* The same assignment (same per-particle arithmetic, same result up to the
+ * order of the float additions) with shared-memory tile accumulation: the
+ * particles are binned by the tile x tile x tile block of cells their stencil
+ * starts in, each block is accumulated in shared memory with its 4-cell halo
+ * and added to the grid once.  Pays off when many particles share cells.
+ * tile: 4, 8 or 16 (ngrid >= tile + 4); np < 2^31.  Scratch: the caller's
+ * workspace of pyspec_assign_tiled_workspace() bytes. */
+size_t pyspec_assign_tiled_workspace(int64_t np, int ngrid, int tile);
+int pyspec_assign_pcs_interlaced_tiled(const float *xyz, const float *w, int64_t np, int ngrid,
+                                       float kf_ks, float offset, int tile, float *grid,
+                                       void *workspace, size_t ws_bytes, void *stream);
+
 /* ------------------------------------------------------------------------
  * 3D complex FFT, in place, unnormalised -- replaces the FFTW plan of
  * pyspectrum.py:1073-1075 (sign=+1, FFTW_BACKWARD, normalise_idft=False) and
@@ -92,6 +108,16 @@ int pyspec_assign_pcs_interlaced(const float *xyz, const float *w, int64_t np, i
  * ngrid must factor into 2, 3 and 5.
  * ---------------------------------------------------------------------- */
 int pyspec_fft3d_c2c(float *grid, int ngrid, int sign, void *stream);
+
+/* Radix-plan variants of the same transform (no counterpart in the
+ * reference; for the autotuner).  pyspec_fft3d_variants returns the number
+ * of variants of ngrid and writes, for each, its two-stage split (r1, r2)
+ * into r1r2[2v], r1r2[2v+1] (up to cap variants; r1r2 may be NULL); (0, 0)
+ * marks the shared-memory Stockham form, which exists for every ngrid.
+ * pyspec_fft3d_c2c_variant runs variant `variant`; all variants compute the
+ * same transform (to float32 rounding). */
+int pyspec_fft3d_variants(int ngrid, int32_t *r1r2, int cap);
+int pyspec_fft3d_c2c_variant(float *grid, int ngrid, int sign, int variant, void *stream);
 
 /* ------------------------------------------------------------------------
  * Interlacing combine, window deconvolution, normalisation -- replaces
@@ -188,6 +214,9 @@ int pyspec_bk_contract(const float *fields, int ngrid, int nshell, const int32_t
  * would; PYSPEC_E_INVALID with a message if the plan fails the check.
  * ---------------------------------------------------------------------- */
 int pyspec_bk_plan_check(int nshell, const int32_t *tri_host, int ntri, int64_t *info, int ninfo);
+/* The same for the plan that method flags `flags` (0 or PYSPEC_CONTRACT_RUN_PLAN) select. */
+int pyspec_bk_plan_check_flags(int nshell, const int32_t *tri_host, int ntri, int flags, int64_t *info,
+                               int ninfo);
 
 /* ------------------------------------------------------------------------
  * Triangle contraction without device allocation.  This entry point has no

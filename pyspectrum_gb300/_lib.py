@@ -28,7 +28,12 @@ SIGNATURES = {
     "pyspec_launch_count": (c_i64, []),
     "pyspec_prepare_positions": (c_int, [_P, c_i64, _P, c_i64, c_int, c_double, _P, c_i64, c_double, _P, _P, _P]),
     "pyspec_assign_pcs_interlaced": (c_int, [_P, _P, c_i64, c_int, c_float, c_float, _P, _P]),
+    "pyspec_assign_tiled_workspace": (c_size, [c_i64, c_int, c_int]),
+    "pyspec_assign_pcs_interlaced_tiled": (c_int, [_P, _P, c_i64, c_int, c_float, c_float, c_int, _P, _P, c_size,
+                                                   _P]),
     "pyspec_fft3d_c2c": (c_int, [_P, c_int, c_int, _P]),
+    "pyspec_fft3d_variants": (c_int, [c_int, _P, c_int]),
+    "pyspec_fft3d_c2c_variant": (c_int, [_P, c_int, c_int, c_int, _P]),
     "pyspec_fcomb_periodic": (c_int, [_P, c_int, c_double, _P, _P]),
     "pyspec_reflect_delta": (c_int, [_P, c_int, _P, _P]),
     "pyspec_half_from_full": (c_int, [_P, c_int, _P, _P]),
@@ -39,6 +44,7 @@ SIGNATURES = {
     "pyspec_bk_contract": (c_int, [_P, c_int, c_int, _P, _P, c_int, c_int, _P, _P, c_size, _P]),
     "pyspec_bk_contract_noalloc": (c_int, [_P, c_int, c_int, _P, c_int, _P, _P]),
     "pyspec_bk_plan_check": (c_int, [c_int, _P, c_int, _P, c_int]),
+    "pyspec_bk_plan_check_flags": (c_int, [c_int, _P, c_int, c_int, _P, c_int]),
     "pyspec_bk_counts_workspace": (c_size, [c_int, c_int, c_int, c_int]),
     "pyspec_bk_counts": (c_int, [c_int, c_int, c_int, c_int, _P, c_int, _P, _P, _P, c_size, _P]),
     "pyspec_bk_normalize": (c_int, [_P, _P, _P, _P, _P, c_int, c_int, c_int, c_int, c_int, c_double, c_double, _P, _P]),
@@ -52,6 +58,7 @@ SIGNATURES = {
 
 CONTRACT_FP32 = 0
 CONTRACT_BF16X3 = 1
+CONTRACT_RUN_PLAN = 0x100
 
 
 class PyspecError(RuntimeError):

@@ -21,7 +21,7 @@ import threading
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, tune
 from ._lib import call, ptr, stream_ptr
 
 METHODS = {"fp32": _lib.CONTRACT_FP32, "bf16x3": _lib.CONTRACT_BF16X3}
@@ -95,9 +95,8 @@ def fft_periodic_half(xyzs: torch.Tensor, ws, Ngrid: int, Lbox: float, wsum: flo
         grid = _assign_grid(n, dev)
     grid.zero_()
     kf_ks = float(np.float32(float(n) / Lbox))          # pyspectrum.py:931
-    call("pyspec_assign_pcs_interlaced", ptr(xyzs), ptr(ws), xyzs.shape[1], n, kf_ks, 0.0,
-         ptr(grid), stream_ptr())
-    call("pyspec_fft3d_c2c", ptr(grid), n, 1, stream_ptr())
+    tune.assign(xyzs, ws, n, kf_ks, 0.0, grid)          # direct or tiled, as tuned for this density
+    tune.fft3d(grid, n, 1)                              # the tuned radix plan
     if half is None:
         half = torch.empty((n, n, n // 2 + 1), dtype=torch.complex64, device=dev)
     call("pyspec_fcomb_periodic", ptr(grid), n, float(wsum), ptr(half), stream_ptr())
@@ -236,15 +235,18 @@ class BkPlan:
         self.out = torch.empty((7, self.T), dtype=torch.float64, device=self.device)
         self.ws_shell = _workspace(lib.pyspec_shell_fields_workspace(n, self.S), self.device)
         self.ws_con = _workspace(lib.pyspec_bk_contract_workspace(n, self.S, self.T, METHODS[method]), self.device)
+        self.contract_flags = None          # tile plan chosen by the tuner at the first contraction
 
     def shells(self, half: torch.Tensor):
         call("pyspec_shell_fields", ptr(half), self.n, self.step, self.jmin, self.nmax, ptr(self.fields),
              ptr(self.p0sum), ptr(self.ws_shell), self.ws_shell.numel(), stream_ptr())
 
     def contract(self):
+        if self.contract_flags is None:
+            self.contract_flags = tune.contract_flags(self)
         call("pyspec_bk_contract", ptr(self.fields), self.n, self.S, ptr(self.slots),
-             self.slots_host.ctypes.data_as(ctypes.c_void_p), self.T, METHODS[self.method], ptr(self.bsum),
-             ptr(self.ws_con), self.ws_con.numel(), stream_ptr())
+             self.slots_host.ctypes.data_as(ctypes.c_void_p), self.T, METHODS[self.method] | self.contract_flags,
+             ptr(self.bsum), ptr(self.ws_con), self.ws_con.numel(), stream_ptr())
 
     def normalize(self, apply_units=False, nbar=1.0, kf=1.0):
         call("pyspec_bk_normalize", ptr(self.bsum), ptr(self.counts), ptr(self.p0sum), ptr(self.nk),

@@ -941,7 +941,7 @@ static bool build_cover_plan(HostPlan* hp, int nshell, const int32_t* tri_host, 
     return true;
 }
 
-static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri) {
+static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri, bool allow_cover) {
     HostPlan* hp = new HostPlan();
     Params& P = hp->base;
     memset(&P, 0, sizeof(P));
@@ -1007,8 +1007,8 @@ static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri) {
     const size_t fixed = (size_t)fixed_smem(nshell);
     const int budget = (int)((227 * 1024 - 8192 - fixed) / sizeof(float2));
     // fewer tiles with a pair cover where the run plan needs 4 (bounded search cost)
-    if (rts.size() > (size_t)RT_PER_GROUP / 2 && rts.size() <= (size_t)RT_PER_GROUP && nshell <= 48 && ntri <= 12000 &&
-        build_cover_plan(hp, nshell, tri_host, ntri, budget, fixed)) {
+    if (allow_cover && rts.size() > (size_t)RT_PER_GROUP / 2 && rts.size() <= (size_t)RT_PER_GROUP && nshell <= 48 &&
+        ntri <= 12000 && build_cover_plan(hp, nshell, tri_host, ntri, budget, fixed)) {
         hp->cover = true;
         return hp;
     }
@@ -1154,13 +1154,16 @@ static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri) {
     return hp;
 }
 
-static HostPlan* get_plan(int nshell, const int32_t* tri_host, int ntri) {
+// run_plan: plan from runs of the triangles' two largest shells even where a
+// pair cover would need fewer tiles (PYSPEC_CONTRACT_RUN_PLAN)
+static HostPlan* get_plan(int nshell, const int32_t* tri_host, int ntri, bool run_plan = false) {
     std::vector<int32_t> key(tri_host, tri_host + 3 * (size_t)ntri);
     key.push_back(nshell);
+    key.push_back(run_plan ? 1 : 0);
     std::lock_guard<std::mutex> lk(g_plan_mu);
     auto it = g_plans.find(key);
     if (it != g_plans.end()) return it->second;
-    HostPlan* hp = build_plan(nshell, tri_host, ntri);
+    HostPlan* hp = build_plan(nshell, tri_host, ntri, !run_plan);
     g_plans[key] = hp;
     return hp;
 }
@@ -1209,13 +1212,13 @@ static EncodeTiledFn encode_tiled() {
 }
 
 int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_t* tri, const int32_t* tri_host,
-                     int ntri, double* bsum, void* ws, size_t ws_bytes, cudaStream_t st) {
+                     int ntri, double* bsum, void* ws, size_t ws_bytes, cudaStream_t st, bool run_plan) {
     using namespace tc;
     PYSPEC_CHECK_ARG(tri_host != nullptr, "the BF16x3 contraction needs the host copy of the triangle list");
     PYSPEC_CHECK_ARG(nvox % 4 == 0, "BF16x3 contraction needs N^3 divisible by 4");
     PYSPEC_CHECK_ARG(nvox / KC + 1 < (int64_t)INT32_MAX / KC, "BF16x3 contraction supports N^3 < 2^31");
     PYSPEC_CHECK_ARG(((uintptr_t)fields & 15) == 0, "fields must be 16-byte aligned");
-    HostPlan* hp = get_plan(nshell, tri_host, ntri);
+    HostPlan* hp = get_plan(nshell, tri_host, ntri, run_plan);
     if (!hp->ok) {
         set_error("%s", hp->why);
         return hp->invalid ? PYSPEC_E_INVALID : PYSPEC_E_UNSUPPORTED;
@@ -1330,11 +1333,17 @@ static bool check_plan(const tc::HostPlan* hp, const int32_t* tri_host, int ntri
 }  // namespace pyspec
 
 extern "C" int pyspec_bk_plan_check(int nshell, const int32_t* tri_host, int ntri, int64_t* info, int ninfo) {
+    return pyspec_bk_plan_check_flags(nshell, tri_host, ntri, 0, info, ninfo);
+}
+
+extern "C" int pyspec_bk_plan_check_flags(int nshell, const int32_t* tri_host, int ntri, int flags, int64_t* info,
+                                          int ninfo) {
     using namespace pyspec;
     using namespace pyspec::tc;
     PYSPEC_CHECK_ARG(tri_host != nullptr && ntri > 0, "empty or NULL triangle list");
     PYSPEC_CHECK_ARG(nshell >= 1 && ninfo >= 0 && (info != nullptr || ninfo == 0), "bad arguments");
-    HostPlan* hp = get_plan(nshell, tri_host, ntri);
+    PYSPEC_CHECK_ARG((flags & ~PYSPEC_CONTRACT_RUN_PLAN) == 0, "unknown plan flags 0x%x", flags);
+    HostPlan* hp = get_plan(nshell, tri_host, ntri, (flags & PYSPEC_CONTRACT_RUN_PLAN) != 0);
     if (!hp->ok) {
         set_error("%s", hp->why);
         return hp->invalid ? PYSPEC_E_INVALID : PYSPEC_E_UNSUPPORTED;

@@ -133,16 +133,67 @@ fft_line_kernel(float2* __restrict__ data, int64_t row_stride, int64_t outer_str
     }
 }
 
-// radix split of the register passes per grid size (0: none)
-constexpr int FR1(int n) { return n == 360 ? 20 : n == 192 ? 16 : n == 256 ? 16 : 0; }
-constexpr int FR2(int n) { return n == 360 ? 18 : n == 192 ? 12 : n == 256 ? 16 : 1; }
+// Radix splits N = R1 * R2 of the register passes, per grid size: variant
+// v < nreg(N) uses split v; variant nreg(N) is the shared-memory Stockham
+// form (every N with factors 2, 3, 5).  The autotuner of the Python layer
+// times them all and picks per N.  Every N listed is a multiple of 8 (the
+// strided passes take 8 whole columns per CTA) and every radix has a
+// small_dft form.
+struct RegSplit { int n, r1, r2; };
+constexpr RegSplit kSplits[] = {
+    {128, 16, 8}, {128, 8, 16},
+    {192, 16, 12}, {192, 12, 16}, {192, 24, 8}, {192, 8, 24},
+    {256, 16, 16},
+    {360, 20, 18}, {360, 18, 20}, {360, 24, 15}, {360, 15, 24},
+};
+constexpr int kNSplits = (int)(sizeof(kSplits) / sizeof(kSplits[0]));
+
+// the variant pyspec_fft3d_c2c uses: the first register split of 192, 256
+// and 360, the Stockham form for every other size
+int fft3d_default_variant(int n) { return (n == 192 || n == 256 || n == 360) ? 0 : fft3d_nreg(n); }
+
+int fft3d_nreg(int n) {
+    int c = 0;
+    for (int k = 0; k < kNSplits; ++k) c += kSplits[k].n == n;
+    return c;
+}
+
+// the (r1, r2) of register variant v of size n, or false
+static bool reg_split(int n, int v, int* r1, int* r2) {
+    for (int k = 0; k < kNSplits; ++k)
+        if (kSplits[k].n == n && v-- == 0) {
+            *r1 = kSplits[k].r1;
+            *r2 = kSplits[k].r2;
+            return true;
+        }
+    return false;
+}
+
+template <int NC, int R1, int R2>
+static int fft3d_reg(float2* d, int n, int sign, cudaStream_t st) {
+    using FS = FftLineShape<NC, R1, R2>;
+    const int64_t lines = (int64_t)n * n;
+    const int ntx = (n + 7) / 8;
+    fft_line_kernel<NC, R1, R2, true><<<(unsigned)(lines / 8), FS::THREADS, 0, st>>>(d, 1, 0, 0, sign);
+    PYSPEC_LAUNCH_CHECK();
+    fft_line_kernel<NC, R1, R2, false><<<(unsigned)(ntx * n), FS::THREADS, 0, st>>>(d, n, (int64_t)n * n, ntx,
+                                                                                    sign);
+    PYSPEC_LAUNCH_CHECK();
+    fft_line_kernel<NC, R1, R2, false><<<(unsigned)(ntx * n), FS::THREADS, 0, st>>>(d, (int64_t)n * n, n, ntx,
+                                                                                    sign);
+    PYSPEC_LAUNCH_CHECK();
+    return PYSPEC_OK;
+}
 
 template <typename T>
-int fft3d_c2c_impl(typename cplx_t<T>::type* data, int n, int sign, cudaStream_t st) {
+int fft3d_c2c_impl(typename cplx_t<T>::type* data, int n, int sign, cudaStream_t st, int variant) {
     using C = typename cplx_t<T>::type;
     RadixPlan plan;
     PYSPEC_CHECK_ARG(make_plan(n, &plan), "ngrid=%d must factor into 2, 3 and 5", n);
     PYSPEC_CHECK_ARG(sign == 1 || sign == -1, "sign must be +1 or -1");
+    const int nreg = sizeof(T) == 4 ? fft3d_nreg(n) : 0;
+    PYSPEC_CHECK_ARG(variant >= 0 && variant <= nreg, "variant %d out of range [0, %d] for ngrid=%d", variant, nreg,
+                     n);
     const int lx = contig_lines(n);
     const size_t sm_c = sizeof(C) * ((size_t)n + 2 * (size_t)lx * n);
     const int64_t lines = (int64_t)n * n;
@@ -150,20 +201,6 @@ int fft3d_c2c_impl(typename cplx_t<T>::type* data, int n, int sign, cudaStream_t
     const int tx = tile_x<T>();
     const int ntx = (n + tx - 1) / tx;
     const size_t sm = sizeof(C) * ((size_t)n + 2 * (size_t)tx * n);
-#define PYSPEC_FFT3D_REG(NCV)                                                                             \
-    do {                                                                                                 \
-        using FS = FftLineShape<NCV, FR1(NCV), FR2(NCV)>;                                                \
-        float2* d = reinterpret_cast<float2*>(data);                                                     \
-        fft_line_kernel<NCV, FR1(NCV), FR2(NCV), true><<<(unsigned)(lines / 8), FS::THREADS, 0, st>>>(    \
-            d, 1, 0, 0, sign);                                                                           \
-        PYSPEC_LAUNCH_CHECK();                                                                           \
-        fft_line_kernel<NCV, FR1(NCV), FR2(NCV), false><<<(unsigned)(ntx * n), FS::THREADS, 0, st>>>(     \
-            d, n, (int64_t)n * n, ntx, sign);                                                            \
-        PYSPEC_LAUNCH_CHECK();                                                                           \
-        fft_line_kernel<NCV, FR1(NCV), FR2(NCV), false><<<(unsigned)(ntx * n), FS::THREADS, 0, st>>>(     \
-            d, (int64_t)n * n, n, ntx, sign);                                                            \
-        PYSPEC_LAUNCH_CHECK();                                                                           \
-    } while (0)
 #define PYSPEC_FFT3D_LAUNCH(NCV)                                                                          \
     do {                                                                                                 \
         PYSPEC_TRY(allow_smem((const void*)fft_contig_kernel<T, NCV>, sm_c));                            \
@@ -175,31 +212,60 @@ int fft3d_c2c_impl(typename cplx_t<T>::type* data, int n, int sign, cudaStream_t
         fft_strided_kernel<T, NCV><<<(unsigned)(ntx * n), 256, sm, st>>>(data, n, (int64_t)n * n, n, plan, sign); \
         PYSPEC_LAUNCH_CHECK();                                                                           \
     } while (0)
-    bool done = false;
+    int r1 = 0, r2 = 0;
     if constexpr (sizeof(T) == 4) {
-        done = true;
-        switch (n) {
-            case 192: PYSPEC_FFT3D_REG(192); break;
-            case 256: PYSPEC_FFT3D_REG(256); break;
-            case 360: PYSPEC_FFT3D_REG(360); break;
-            case 512: PYSPEC_FFT3D_LAUNCH(512); break;
-            default: done = false;
+        if (variant < nreg && reg_split(n, variant, &r1, &r2)) {
+            float2* d = reinterpret_cast<float2*>(data);
+            int rc = PYSPEC_E_UNSUPPORTED;
+#define PYSPEC_FFT3D_REG(NV, A, B) \
+    if (n == NV && r1 == A && r2 == B) rc = fft3d_reg<NV, A, B>(d, n, sign, st);
+            PYSPEC_FFT3D_REG(128, 16, 8) PYSPEC_FFT3D_REG(128, 8, 16)
+            PYSPEC_FFT3D_REG(192, 16, 12) PYSPEC_FFT3D_REG(192, 12, 16) PYSPEC_FFT3D_REG(192, 24, 8)
+            PYSPEC_FFT3D_REG(192, 8, 24)
+            PYSPEC_FFT3D_REG(256, 16, 16)
+            PYSPEC_FFT3D_REG(360, 20, 18) PYSPEC_FFT3D_REG(360, 18, 20) PYSPEC_FFT3D_REG(360, 24, 15)
+            PYSPEC_FFT3D_REG(360, 15, 24)
+#undef PYSPEC_FFT3D_REG
+            PYSPEC_TRY(rc);
+            count_launch(3);
+            return PYSPEC_OK;
         }
     }
-    if (!done) PYSPEC_FFT3D_LAUNCH(0);
+    if (n == 512) PYSPEC_FFT3D_LAUNCH(512);
+    else PYSPEC_FFT3D_LAUNCH(0);
 #undef PYSPEC_FFT3D_LAUNCH
-#undef PYSPEC_FFT3D_REG
     count_launch(3);
     return PYSPEC_OK;
 }
 
-template int fft3d_c2c_impl<float>(float2*, int, int, cudaStream_t);
-template int fft3d_c2c_impl<double>(double2*, int, int, cudaStream_t);
+template int fft3d_c2c_impl<float>(float2*, int, int, cudaStream_t, int);
+template int fft3d_c2c_impl<double>(double2*, int, int, cudaStream_t, int);
 
 }  // namespace pyspec
 
 extern "C" int pyspec_fft3d_c2c(float* grid, int ngrid, int sign, void* stream) {
     PYSPEC_CHECK_ARG(grid != nullptr, "grid is NULL");
     PYSPEC_CHECK_ARG(ngrid >= 2 && ngrid <= 2048, "ngrid=%d out of range", ngrid);
-    return pyspec::fft3d_c2c_impl<float>(reinterpret_cast<float2*>(grid), ngrid, sign, pyspec::as_stream(stream));
+    return pyspec::fft3d_c2c_impl<float>(reinterpret_cast<float2*>(grid), ngrid, sign, pyspec::as_stream(stream),
+                                         pyspec::fft3d_default_variant(ngrid));
+}
+
+extern "C" int pyspec_fft3d_variants(int ngrid, int32_t* r1r2, int cap) {
+    const int nreg = pyspec::fft3d_nreg(ngrid);
+    for (int v = 0; v <= nreg && v < cap; ++v) {
+        int a = 0, b = 0;
+        if (v < nreg) pyspec::reg_split(ngrid, v, &a, &b);
+        if (r1r2 != nullptr) {
+            r1r2[2 * v] = a;
+            r1r2[2 * v + 1] = b;
+        }
+    }
+    return nreg + 1;
+}
+
+extern "C" int pyspec_fft3d_c2c_variant(float* grid, int ngrid, int sign, int variant, void* stream) {
+    PYSPEC_CHECK_ARG(grid != nullptr, "grid is NULL");
+    PYSPEC_CHECK_ARG(ngrid >= 2 && ngrid <= 2048, "ngrid=%d out of range", ngrid);
+    return pyspec::fft3d_c2c_impl<float>(reinterpret_cast<float2*>(grid), ngrid, sign, pyspec::as_stream(stream),
+                                         variant);
 }

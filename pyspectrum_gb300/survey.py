@@ -14,7 +14,7 @@ from __future__ import annotations
 import numpy as np
 import torch
 
-from . import _lib, core
+from . import _lib, core, tune
 from ._lib import call, ptr, stream_ptr
 from .util import FlatLambdaCDM, radecz_to_cartesian
 
@@ -53,8 +53,8 @@ def _fft_survey_half(radecz, nb, w=None, P0_fkp=1e6, Lbox=2600.0, Ngrid=360, cos
     call("pyspec_cast_positions", ptr(x_d), x_d.stride(0), ptr(w_d), N, ptr(xyzs), ptr(ws), stream_ptr())
     grid = torch.zeros((n, n, n), dtype=torch.complex64, device=dev)
     kf_ks = float(np.float32(float(n) / Lbox))        # pyspectrum.py:773
-    call("pyspec_assign_pcs_interlaced", ptr(xyzs), ptr(ws), N, n, kf_ks, 0.5 * n, ptr(grid), stream_ptr())
-    call("pyspec_fft3d_c2c", ptr(grid), n, 1, stream_ptr())
+    tune.assign(xyzs, ws, n, kf_ks, 0.5 * n, grid)      # offset N/2 cells (pyspectrum.py:775)
+    tune.fft3d(grid, n, 1)
     half = torch.empty((n, n, n // 2 + 1), dtype=torch.complex64, device=dev)
     call("pyspec_fcomb_survey", ptr(grid), n, ptr(half), stream_ptr())
     return half, Ntot, I12, I13, I22, I23, I33
