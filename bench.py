@@ -473,17 +473,25 @@ def run_gpu(args, rank, world, local_rank):
             "e2e": {"value": job_rate(world, e2e_steps, e2e_s), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "api": "pyspectrum_gb300.pyspectrum.Bk_periodic(pinned xyz)"},
             "gpu_launches": main["gpu_launches"], "clocks": main["clocks"], "fft3d_comparator": fftcmp}
+    from pyspectrum_gb300 import tune
+    line["tuned"] = {k.split("|", 2)[0] + "|" + k.split("|", 2)[2]: v for k, v in tune.choices().items()}
+    if not args.no_batch:
+        try:
+            line["batch_64_mocks"] = batch_rate()
+        except Exception as exc:        # informational; the headline line still prints
+            line["batch_64_mocks"] = {"error": str(exc)[:300]}
     print(json.dumps(line), flush=True)
 
 
-def run_batch(args):
-    """Many boxes per call (Bk_periodic_batch): 64 seeded Zel'dovich mocks with
-    particle counts uniform in [0.5M, 4M] and grids mixed over {192, 256, 360}
-    (L = 2500, step 3, Nmax 40, split-BF16).  Prints one JSON line with the
-    batch time (positions already in pinned host memory; results back on the
-    host); not the headline bench line."""
+def batch_rate():
+    """Many boxes per call (Bk_periodic_batch), the many-mock workload: 64
+    seeded Zel'dovich mocks with particle counts uniform in [0.5M, 4M] and
+    grids mixed over {192, 256, 360} (L = 2500, step 3, Nmax 40, split-BF16,
+    graph replay).  Positions start in pinned host memory and the results end
+    on the host.  The first pass (plans, counts, tuning, graph capture of the
+    three geometries) is untimed; the second is timed by the host clock."""
     import torch
-    from pyspectrum_gb300 import batch, mocks
+    from pyspectrum_gb300 import batch, mocks, tune
     rng = np.random.default_rng(4)
     L = 2500.0
     nmock = 64
@@ -495,20 +503,74 @@ def run_batch(args):
         cat.append((torch.from_numpy(x.cpu().numpy()).pin_memory(), int(grids[k])))
         del x
     runner = batch.BkBatch(Lbox=L, step=3, Ncut=3, Nmax=40, method="bf16x3", graphs=True)
-    # first pass: plans, counts and graph capture for the three geometries
     warm = [cat[int(np.nonzero(grids == g)[0][0])] for g in (192, 256, 360) for _ in range(2)]
     runner.run(warm)
+    runner.run(cat)                      # tunes the assignment at every density bucket met
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     out = runner.run(cat)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     assert len(out) == nmock and all(np.isfinite(o["b123"]).all() for o in out)
-    line = {"workload": "64 Zel'dovich mocks, Np in [0.5M, 4M], Ngrid in {192, 256, 360}, L 2500, step 3, Nmax 40",
-            "metric": "Bk evals/s (batch, host positions in, host results out)", "value": nmock / dt,
-            "seconds": dt, "mocks_per_grid": {str(g): int((grids == g).sum()) for g in (192, 256, 360)},
-            "particles_total": int(nparts.sum()), "method": "bf16x3", "graphs": True}
-    print(json.dumps(line), flush=True)
+    tuned = {k.split("|", 2)[0] + "|" + k.split("|", 2)[2]: v["choice"] for k, v in tune.choices().items()}
+    return {"workload": "64 Zel'dovich mocks, Np uniform in [0.5M, 4M], Ngrid in {192, 256, 360}, L 2500, step 3, "
+                        "Nmax 40", "metric": "Bk evals/s (batch, pinned host positions in, host results out)",
+            "value": nmock / dt, "seconds": dt, "mocks_per_grid": {str(g): int((grids == g).sum()) for g in
+                                                                   (192, 256, 360)},
+            "particles_total": int(nparts.sum()), "method": "bf16x3", "graphs": True, "tuned": tuned}
+
+
+def run_batch(args):
+    """Prints the many-mock batch line alone (not the headline bench line)."""
+    print(json.dumps(batch_rate()), flush=True)
+
+
+def run_profile_delta(reps=3):
+    """Profiling case for the delta(k) and P(k) kernels on the bench workload
+    (1M particles, 360^3): `reps` rounds of clip/cast, the direct and the
+    8^3-tiled mass assignment, the 3D FFT (default radix plan), the
+    interlacing combine, the P(k) monopole and the pk_pbox_rsd multipoles.
+    About 1.2 GB on the device; prints the last round's event times (not a
+    bench result)."""
+    import torch
+    from pyspectrum_gb300 import _lib, core
+    from pyspectrum_gb300._lib import call, ptr, stream_ptr
+    W = WORKLOAD
+    n, L = W["Ngrid"], W["Lbox"]
+    x = torch.from_numpy(make_positions_np()).cuda()
+    npart = x.shape[1]
+    grid = torch.zeros((n, n, n), dtype=torch.complex64, device="cuda")
+    half = torch.empty((n, n, n // 2 + 1), dtype=torch.complex64, device="cuda")
+    kf_ks = float(np.float32(float(n) / L))
+    wst = torch.empty(_lib.load().pyspec_assign_tiled_workspace(npart, n, 8), dtype=torch.uint8, device="cuda")
+    nbin, nmu = n // 2, 10
+    pko = torch.empty(6 * nbin, dtype=torch.float64, device="cuda")
+    rso = torch.empty(2 * (5 * nbin + 4 * nbin * nmu), dtype=torch.float64, device="cuda")
+    names = ["prepare", "assign_direct", "assign_tiled8", "fft3d", "fcomb", "pk_mono", "pk_rsd"]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(names) + 1)]
+    for _ in range(reps):
+        ev[0].record()
+        xyzs, ws = core.prepare_positions(x, L)
+        ev[1].record()
+        grid.zero_()
+        call("pyspec_assign_pcs_interlaced", ptr(xyzs), ptr(ws), npart, n, kf_ks, 0.0, ptr(grid), stream_ptr())
+        ev[2].record()
+        grid.zero_()
+        call("pyspec_assign_pcs_interlaced_tiled", ptr(xyzs), ptr(ws), npart, n, kf_ks, 0.0, 8, ptr(grid),
+             ptr(wst), wst.numel(), stream_ptr())
+        ev[3].record()
+        call("pyspec_fft3d_c2c", ptr(grid), n, 1, stream_ptr())
+        ev[4].record()
+        call("pyspec_fcomb_periodic", ptr(grid), n, float(npart), ptr(half), stream_ptr())
+        ev[5].record()
+        call("pyspec_pk_monopole", ptr(half), n, float(L), ptr(pko), stream_ptr())
+        ev[6].record()
+        call("pyspec_pk_pbox_rsd", ptr(half), n, 2, int(L), nbin, nmu, ptr(rso), stream_ptr())
+        ev[7].record()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "delta_k_and_pk", "Ngrid": n, "npart": npart,
+                      "ms_last_round": {nm: ev[k].elapsed_time(ev[k + 1]) for k, nm in enumerate(names)}}),
+          flush=True)
 
 
 def run_profile_shells(jtop):
@@ -549,13 +611,19 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-check", action="store_true", help="skip the float64 error check of all triangles")
     ap.add_argument("--small", action="store_true", help="run the 192^3 profiling case instead of the bench workload")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-mock batch measurement on the main line")
     ap.add_argument("--batch", action="store_true",
                     help="time 64 mixed-size mocks through Bk_periodic_batch instead of the bench workload")
+    ap.add_argument("--profile-delta", action="store_true",
+                    help="only run the delta(k) and P(k) kernels of the bench workload (ncu profiling case)")
     ap.add_argument("--profile-shells", type=int, default=0, metavar="J",
                     help="only run shells J-2..J of the bench workload three times (ncu profiling case)")
     args = ap.parse_args()
     if args.profile_shells:
         run_profile_shells(args.profile_shells)
+        return
+    if args.profile_delta:
+        run_profile_delta()
         return
     if args.batch:
         run_batch(args)
