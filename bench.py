@@ -474,7 +474,8 @@ def run_gpu(args, rank, world, local_rank):
                     "d2h_bytes_per_step": d2h, "api": "pyspectrum_gb300.pyspectrum.Bk_periodic(pinned xyz)"},
             "gpu_launches": main["gpu_launches"], "clocks": main["clocks"], "fft3d_comparator": fftcmp}
     from pyspectrum_gb300 import tune
-    line["tuned"] = {k.split("|", 2)[0] + "|" + k.split("|", 2)[2]: v for k, v in tune.choices().items()}
+    line["tuned"] = {k.split("|", 2)[0] + "|" + k.split("|", 2)[2]: v for k, v in tune.choices().items()
+                     if f"|n{n}|" in k}
     if not args.no_batch:
         try:
             line["batch_64_mocks"] = batch_rate()
@@ -512,7 +513,8 @@ def batch_rate():
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     assert len(out) == nmock and all(np.isfinite(o["b123"]).all() for o in out)
-    tuned = {k.split("|", 2)[0] + "|" + k.split("|", 2)[2]: v["choice"] for k, v in tune.choices().items()}
+    tuned = {k.split("|", 2)[0] + "|" + k.split("|", 2)[2]: v["choice"] for k, v in tune.choices().items()
+             if any(f"|n{g}|" in k for g in (192, 256, 360))}
     return {"workload": "64 Zel'dovich mocks, Np uniform in [0.5M, 4M], Ngrid in {192, 256, 360}, L 2500, step 3, "
                         "Nmax 40", "metric": "Bk evals/s (batch, pinned host positions in, host results out)",
             "value": nmock / dt, "seconds": dt, "mocks_per_grid": {str(g): int((grids == g).sum()) for g in

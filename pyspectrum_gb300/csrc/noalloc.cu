@@ -73,13 +73,21 @@ extern "C" int pyspec_bk_contract_noalloc(const float* fields, int ngrid, int ns
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     PYSPEC_CUDA(cudaStreamIsCapturing(as_stream(stream), &cap));
     const bool capturing = cap != cudaStreamCaptureStatusNone;
-    // the scratch this list needs, from its tile plan (planned here unless the
-    // stream is capturing, where only an existing plan may be used)
+    // an upper bound of the scratch from the sizes alone (partial sums of
+    // every CTA and the largest tile tables a list of ntri triangles can
+    // need): requests beyond the array are refused before any planning
+    const size_t bound = contract_fp32_ws(V, nshell, ntri);
+    if (bound > (size_t)PYSPEC_NOALLOC_SCRATCH_BYTES) {
+        set_error("this contraction may need up to %zu bytes of scratch; the fixed scratch array holds %zu "
+                  "(use pyspec_bk_contract with a workspace)", bound, (size_t)PYSPEC_NOALLOC_SCRATCH_BYTES);
+        return PYSPEC_E_INVALID;
+    }
+    // the list's tile plan: built here, or, while the stream is capturing,
+    // only taken from the cache (its exact scratch never exceeds the bound)
     size_t need = 0;
     PYSPEC_TRY(contract_fp32_need(V, nshell, tri_host, ntri, !capturing, &need));
-    if (need > (size_t)PYSPEC_NOALLOC_SCRATCH_BYTES) {
-        set_error("this contraction needs %zu bytes of scratch; the fixed scratch array holds %zu "
-                  "(use pyspec_bk_contract with a workspace)", need, (size_t)PYSPEC_NOALLOC_SCRATCH_BYTES);
+    if (need > bound) {
+        set_error("internal: planned scratch %zu bytes exceeds its bound %zu", need, bound);
         return PYSPEC_E_INVALID;
     }
     void* scratch = nullptr;

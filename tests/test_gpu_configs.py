@@ -103,7 +103,7 @@ def test_config1_uniform_128_end_to_end():
     craw, _ = TF.triangle_sums(I, tri - jmin, with_abs=False)
     del I, ind
     counts = np.rint(craw / float(n) ** 3).astype(np.int64)
-    assert np.abs(craw / float(n) ** 3 - counts).max() < 1e-6
+    assert np.abs(craw / float(n) ** 3 - counts).max() < 1e-3      # float64 sums of ~1e11: integers to ~1e-5
     assert int((counts > 0).sum()) == 4420
     nk = O.mode_counts(n, step, nmax)
     assert nk[38:41].sum() == 0                         # shells 38-40 are empty at 128^3

@@ -55,16 +55,22 @@ def test_tiled_assignment_matches_direct_and_oracle(n, L, offset_cells, clustere
     kf = float(np.float32(n / L))
     xyz32 = torch.from_numpy(xyz.astype(np.float32)).cuda()
     w32 = None if w is None else torch.from_numpy(w.astype(np.float32)).cuda()
-    ref = _assign("direct", xyz32, w32, n, kf, offset_cells)
-    scale = np.abs(ref).max()
-    for kind in ("tiled4", "tiled8", "tiled16"):
-        got = _assign(kind, xyz32, w32, n, kf, offset_cells)
-        np.testing.assert_allclose(got, ref, rtol=0, atol=2e-6 * scale, err_msg=kind)
-    # the oracle (float64 sums of the same single-precision weights)
+    # the oracle: float64 sums of the same single-precision weights.  Every
+    # device variant sums in float32 in its own order; a cell with m
+    # contributions is within ~m ulp of the exact sum (dense clusters put
+    # thousands of particles in a cell), hence the relative tolerance.
     xyz_f = np.asfortranarray(xyz.astype(np.float32))
     g = O.assign_quad(xyz_f, None if w is None else w.astype(np.float32), np.float32(kf), offset_cells, n)
     ora = np.stack([g.real, g.imag], axis=-1).transpose(2, 1, 0, 3)     # [z, y, x, re/im]
-    np.testing.assert_allclose(ref, ora, rtol=0, atol=2e-6 * scale)
+    scale = np.abs(ora).max()
+    ref = _assign("direct", xyz32, w32, n, kf, offset_cells)
+    np.testing.assert_allclose(ref, ora, rtol=2e-5, atol=2e-7 * scale, err_msg="direct")
+    for kind in ("tiled4", "tiled8", "tiled16"):
+        got = _assign(kind, xyz32, w32, n, kf, offset_cells)
+        np.testing.assert_allclose(got, ora, rtol=2e-5, atol=2e-7 * scale, err_msg=kind)
+        np.testing.assert_allclose(got, ref, rtol=4e-5, atol=4e-7 * scale, err_msg=kind)
+        # the cells touched are exactly the same
+        np.testing.assert_array_equal(got != 0, ref != 0, err_msg=kind)
     # mass: every particle deposits its weight (x 6^3 per grid) on both grids
     tot = ref.sum(axis=(0, 1, 2)) / 216.0
     wsum = npart if w is None else float(np.sum(w.astype(np.float32)))
