@@ -84,6 +84,25 @@ def plan_macs_per_voxel(nmax, ncut, step):
     return int(info[6])
 
 
+def fp32_tiles(nmax, ncut, step):
+    """Micro-tiles (4 pair rows x 8 shells) of the FP32 contraction's plan for
+    the triangle loop: pairs (i, j) sorted by (j, i) in groups of 4, one tile
+    per 8-wide window of l between the group's lowest and highest l."""
+    jmin = ncut // step
+    pairs = {}
+    for i in range(jmin, nmax + 1):
+        for j in range(jmin, i + 1):
+            for l in range(max(i - j, jmin), j + 1):
+                pairs.setdefault((i - jmin, j - jmin), []).append(l - jmin)
+    order = sorted(pairs, key=lambda p: (p[1], p[0]))
+    tiles = 0
+    for g in range(0, len(order), 4):
+        ls = [l for p in order[g:g + 4] for l in pairs[p]]
+        lo, hi = min(ls), max(ls)
+        tiles += (hi - lo) // 8 + 1
+    return tiles
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -326,7 +345,7 @@ def run_gpu(args, rank, world, local_rank):
     grid = torch.zeros((n, n, n), dtype=torch.complex64, device=dev)
     half = torch.empty((n, n, n // 2 + 1), dtype=torch.complex64, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
-    plans = {m: core.get_plan(n, step, ncut, nmax, m, dev) for m in ("bf16x3", "fp32")}
+    plans = {m: core.get_plan(n, step, ncut, nmax, m, dev) for m in ("bf16x3", "fp32", "bf16x3_fine")}
 
     def step_fn(plan, ev=None):
         if ev is not None:
@@ -350,7 +369,7 @@ def run_gpu(args, rank, world, local_rank):
             dist.barrier()
 
     results = {}
-    for method in ("bf16x3", "fp32"):
+    for method in ("bf16x3", "fp32", "bf16x3_fine"):
         plan = plans[method]
         steps = args.steps if method == "bf16x3" else max(1, min(args.steps, 5))
         for _ in range(args.warmup):
@@ -375,7 +394,7 @@ def run_gpu(args, rank, world, local_rank):
         results[method] = {"ms_per_step": ms / steps, "bk_evals_per_s": job_rate(world, steps, ms / 1e3),
                            "triangles_per_s": plan.T / (stage["contraction"] / 1e3), "stage_ms": stage,
                            "gpu_launches": launches, "steps": steps, "clocks": clk.summary()}
-        if method == "bf16x3":
+        if method in core.TENSOR_METHODS:
             results[method]["status_word"] = int(plan.ws_con[:4].view(torch.int32).item())
 
     # timing comparator for the 3D FFT (cuFFT through torch.fft): the same
@@ -450,6 +469,15 @@ def run_gpu(args, rank, world, local_rank):
                 "useful_over_executed": useful / executed,
                 "traffic": 4.0 * 40 * V, "traffic_note": "dram bytes of one launch: the ncu capture at 192^3 "
                 "(1.133 GB read) scaled by the voxel count; equal to the algorithmic bytes (fields read once)"}
+    # the FP32 CUDA-core comparator against the FP32 SIMT peak (nominal: 152
+    # SMs x 128 FP32 lanes x 2 FLOP x 2.07 GHz; no measured FP32 peak exists)
+    t32 = results["fp32"]["stage_ms"]["contraction"] / 1e3
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+    results["fp32"]["roofline"] = {
+        "kernel": "contract_fp32_kernel (+ partial reduction)", "bound": "fp32 simt", "unit": "TFLOP/s",
+        "achieved": useful / t32 / 1e12, "peak": fp32_peak, "peak_kind": "nominal", "frac": useful / t32 / 1e12 / fp32_peak,
+        "executed_tflops": 2.0 * 32 * fp32_tiles(nmax, ncut, step) * V / t32 / 1e12,
+        "note": "executed = 2 FLOP x 32 products per micro-tile (4 pairs x 8 shells) x tiles x voxels"}
     cpu = None
     if not args.no_cpu_baseline:
         from oracle import cpu_ref
@@ -575,6 +603,41 @@ def run_profile_delta(reps=3):
           flush=True)
 
 
+def run_assign_sweep():
+    """The mass-assignment variants (direct L2 atomics; shared-memory tiles of
+    4^3, 8^3, 16^3 cells) timed at three densities of Zel'dovich boxes: the
+    bench box (1M particles on 360^3), the densest mock of the many-mock
+    workload (4M on 192^3) and the large grid (16M on 512^3).  Best of 5
+    CUDA-event timings each (the grid zeroing excluded).  Prints one JSON line."""
+    import torch
+    from pyspectrum_gb300 import core, mocks, tune
+    out = {}
+    for n, npart, L in ((360, 1_000_000, 2500.0), (192, 4_000_000, 2500.0), (512, 16_000_000, 3000.0)):
+        x = mocks.zeldovich_mock(npart, L, ngrid=n, seed=5)
+        xyzs, ws = core.prepare_positions(x, L)
+        del x
+        grid = torch.zeros((n, n, n), dtype=torch.complex64, device="cuda")
+        kf_ks = float(np.float32(float(n) / L))
+        wsbuf = {b: tune._assign_workspace(npart, n, b, grid.device) for b in (4, 8, 16)}
+        res = {}
+        for c in tune.assign_candidates(n):
+            best = float("inf")
+            for _ in range(6):
+                grid.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                tune._assign_run(c, xyzs, ws, n, kf_ks, 0.0, grid, wsbuf)
+                e1.record()
+                e1.synchronize()
+                best = min(best, e0.elapsed_time(e1))
+            res[c] = round(best, 4)
+        out[f"{npart // 1_000_000}M_on_{n}^3"] = {"particles_per_cell": npart / n ** 3, "ms": res,
+                                                   "fastest": min(res, key=res.get)}
+        del xyzs, ws, grid, wsbuf
+        torch.cuda.empty_cache()
+    print(json.dumps({"assign_sweep": out}), flush=True)
+
+
 def run_profile_shells(jtop):
     """Profiling case for the shell passes: shells jtop-2..jtop of the bench
     workload's delta(k) at 360^3 (about 1 GB on the device), three calls.
@@ -616,6 +679,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-mock batch measurement on the main line")
     ap.add_argument("--batch", action="store_true",
                     help="time 64 mixed-size mocks through Bk_periodic_batch instead of the bench workload")
+    ap.add_argument("--assign-sweep", action="store_true",
+                    help="only time the mass-assignment variants at three particle densities")
     ap.add_argument("--profile-delta", action="store_true",
                     help="only run the delta(k) and P(k) kernels of the bench workload (ncu profiling case)")
     ap.add_argument("--profile-shells", type=int, default=0, metavar="J",
@@ -626,6 +691,9 @@ def main():
         return
     if args.profile_delta:
         run_profile_delta()
+        return
+    if args.assign_sweep:
+        run_assign_sweep()
         return
     if args.batch:
         run_batch(args)

@@ -52,6 +52,11 @@ extern "C" {
  * each triangle's two largest shells even where a pair cover would need
  * fewer tiles (same sums; for the autotuner, which times both plans). */
 #define PYSPEC_CONTRACT_RUN_PLAN 0x100
+/* Flag OR-ed into the BF16X3 method: drain the tensor-memory FP32
+ * accumulators into the compensated sums every 8 chunks of 32 voxels instead
+ * of every 32.  The split-BF16 error is set by the length of that FP32
+ * accumulation, so this trades drain time for about 4x smaller errors. */
+#define PYSPEC_CONTRACT_FINE_DRAIN 0x200
 
 int pyspec_abi_version(void);
 

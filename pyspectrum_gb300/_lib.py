@@ -59,6 +59,7 @@ SIGNATURES = {
 CONTRACT_FP32 = 0
 CONTRACT_BF16X3 = 1
 CONTRACT_RUN_PLAN = 0x100
+CONTRACT_FINE_DRAIN = 0x200
 
 
 class PyspecError(RuntimeError):

@@ -125,7 +125,7 @@ class BkBatch:
             host = torch.empty(geo.plan.out.shape, dtype=torch.float64, pin_memory=True)
             host.copy_(geo.plan.out, non_blocking=True)
             status = None
-            if self.method == "bf16x3":     # the contraction's status word of this mock
+            if self.method in core.TENSOR_METHODS:     # the contraction's status word of this mock
                 status = torch.empty(1, dtype=torch.int32, pin_memory=True)
                 status.copy_(geo.plan.status_word(), non_blocking=True)
             ev = torch.cuda.Event()

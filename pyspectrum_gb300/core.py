@@ -24,7 +24,12 @@ import torch
 from . import _lib, tune
 from ._lib import call, ptr, stream_ptr
 
-METHODS = {"fp32": _lib.CONTRACT_FP32, "bf16x3": _lib.CONTRACT_BF16X3}
+# contraction methods: FP32 CUDA cores; split-BF16 tensor cores with the
+# accumulators drained every 32 chunks ('bf16x3') or every 8 ('bf16x3_fine':
+# about 4x smaller error, the drains cost more time)
+METHODS = {"fp32": _lib.CONTRACT_FP32, "bf16x3": _lib.CONTRACT_BF16X3,
+           "bf16x3_fine": _lib.CONTRACT_BF16X3 | _lib.CONTRACT_FINE_DRAIN}
+TENSOR_METHODS = ("bf16x3", "bf16x3_fine")
 
 
 def _dev(device=None) -> torch.device:
@@ -270,7 +275,7 @@ class BkPlan:
         Only triangles with counts > 0 are returned (all arrays aligned).
         Raises ContractTimeout if the tensor-core contraction stopped early."""
         out = self.out.cpu().numpy()
-        if self.method == "bf16x3":
+        if self.method in TENSOR_METHODS:
             check_contract_status(self.status_word().item())
         keep = self.counts_np > 0
         tri = self.tri_np[:, keep]

@@ -641,7 +641,7 @@ extern "C" int pyspec_bk_normalize(const double* bsum, const int64_t* counts, co
 }
 
 extern "C" size_t pyspec_bk_contract_workspace(int ngrid, int nshell, int ntri, int method) {
-    method &= ~PYSPEC_CONTRACT_RUN_PLAN;
+    method &= ~(PYSPEC_CONTRACT_RUN_PLAN | PYSPEC_CONTRACT_FINE_DRAIN);
     if (ngrid < 2 || nshell < 1 || ntri < 0) return 0;
     const int64_t V = (int64_t)ngrid * ngrid * ngrid;
     if (method == PYSPEC_CONTRACT_BF16X3) return contract_tc_ws(V, nshell, ntri);
@@ -662,8 +662,10 @@ extern "C" int pyspec_bk_contract(const float* fields, int ngrid, int nshell, co
     }
     cudaStream_t st = as_stream(stream);
     const bool run_plan = (method & PYSPEC_CONTRACT_RUN_PLAN) != 0;
-    method &= ~PYSPEC_CONTRACT_RUN_PLAN;
-    PYSPEC_CHECK_ARG(!run_plan || method == PYSPEC_CONTRACT_BF16X3, "PYSPEC_CONTRACT_RUN_PLAN applies to BF16X3 only");
+    const bool fine_drain = (method & PYSPEC_CONTRACT_FINE_DRAIN) != 0;
+    method &= ~(PYSPEC_CONTRACT_RUN_PLAN | PYSPEC_CONTRACT_FINE_DRAIN);
+    PYSPEC_CHECK_ARG((!run_plan && !fine_drain) || method == PYSPEC_CONTRACT_BF16X3,
+                     "PYSPEC_CONTRACT_RUN_PLAN and PYSPEC_CONTRACT_FINE_DRAIN apply to BF16X3 only");
     if (method == PYSPEC_CONTRACT_FP32) {
         if (tri_host == nullptr)   // device-only triangle list: the unplanned kernel
             return contract_simple_impl<float>(fields, V, nshell, tri, ntri, nullptr, V, bsum,
@@ -671,7 +673,8 @@ extern "C" int pyspec_bk_contract(const float* fields, int ngrid, int nshell, co
         return contract_fp32_impl(fields, V, nshell, tri_host, ntri, bsum, workspace, ws_bytes, st);
     }
     if (method == PYSPEC_CONTRACT_BF16X3)
-        return contract_tc_impl(fields, V, nshell, tri, tri_host, ntri, bsum, workspace, ws_bytes, st, run_plan);
+        return contract_tc_impl(fields, V, nshell, tri, tri_host, ntri, bsum, workspace, ws_bytes, st, run_plan,
+                                fine_drain);
     set_error("unknown contraction method %d", method);
     return PYSPEC_E_INVALID;
 }

@@ -21,7 +21,8 @@ int contract_fp32_need(int64_t nvox, int nshell, const int32_t* tri_host, int nt
 // tcgen05 split-BF16 contraction (contract_tc.cu)
 size_t contract_tc_ws(int64_t nvox, int nshell, int ntri);
 int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_t* tri, const int32_t* tri_host,
-                     int ntri, double* bsum, void* ws, size_t ws_bytes, cudaStream_t st, bool run_plan = false);
+                     int ntri, double* bsum, void* ws, size_t ws_bytes, cudaStream_t st, bool run_plan = false,
+                     bool fine_drain = false);
 
 // bsum[t] = sum over nblk rows of partials[b][t] (float64, fixed order)
 int reduce_partials_launch(const double* partials, int nblk, int ntri, double* bsum, cudaStream_t st);

@@ -36,7 +36,8 @@
 //   warp 17, lane 0: streams the fields: one TMA tensor copy per chunk
 //     (nshell rows x 32 floats, 128-byte swizzle) into a ring of NFBUF
 //     buffers, completing on `ffull[buffer]`.
-//   Every SEG chunks the accumulators are drained: the MMA thread commits to
+//   Every 2^seg_log2 chunks (32; 8 with PYSPEC_CONTRACT_FINE_DRAIN) the
+//   accumulators are drained: the MMA thread commits to
 //   `seg`, the producers add the TMEM accumulators into Kahan-compensated
 //   float32 sums per triangle in shared memory and arrive on `drained`; the
 //   next MMA restarts the accumulators.  At the end each CTA writes one float64
@@ -69,7 +70,8 @@ constexpr int PWARPS = NPROD / 32;
 constexpr int MMA_WARP = PWARPS;
 constexpr int TMA_WARP = PWARPS + 1;
 constexpr int NTHREADS = NPROD + 64; // + the MMA warp + the copy warp
-constexpr int SEG = 32;              // chunks between accumulator drains (TMEM float32 accumulation length sets the error: 128 chunks gave a bf16x3 median error of 8e-6 vs FP64, 64 gave 4e-6)
+constexpr int SEG_LOG2 = 5;          // default: drain every 32 chunks (the TMEM float32 accumulation length sets the error: 128 chunks gave a bf16x3 median error of 8e-6 vs FP64, 64 gave 4e-6)
+constexpr int SEG_LOG2_FINE = 3;     // PYSPEC_CONTRACT_FINE_DRAIN: every 8 chunks
 constexpr int MAXGROUPS = 8;
 constexpr int MAXTILES = 4;
 constexpr int RT_PER_GROUP = 64;     // producer row threads per group: 2 tile pairs x 4 lane quarters x 8
@@ -112,6 +114,7 @@ struct Params {
     const int32_t* slot_tri;     // [group][maxslots] triangle index of each slot (-1: unused)
     double* partials;            // [gridDim.x][ntri]
     int* err;
+    int seg_log2;                // accumulators drained every 2^seg_log2 chunks
     int ngroups;
     int maxslots;
     Group g[MAXGROUPS];
@@ -408,7 +411,8 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
             ub_g = (gtid >= nsh) + (gtid >= 2 * nsh) + (gtid >= 3 * nsh);
             ub_r = gtid - ub_g * nsh;
         }
-        const int nseg = (nch + SEG - 1) / SEG;
+        const int seg_len = 1 << P.seg_log2;
+        const int nseg = (nch + seg_len - 1) >> P.seg_log2;
         int seg_count = 0;
         bool failed = false;
         // drain the accumulators of segment seg_count (all warps of both groups)
@@ -509,7 +513,7 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
             // a segment that ended before this chunk is drained after the
             // chunk is produced: its MMAs (which wait for the drain) can then
             // start as soon as the drain ends
-            while (seg_count < nseg && (seg_count + 1) * SEG - 1 < c) {
+            while (seg_count < nseg && ((seg_count + 1) << P.seg_log2) - 1 < c) {
                 if (!drain()) { atomicExch(P.err, 2); abort_flag = 1; failed = true; break; }
             }
             if (failed) break;
@@ -538,6 +542,7 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
             // tile count 2, 3 or 4 and the form select one branch-free sequence
             const int mode = (wide ? 3 : 0) + (ntiles == 2 ? 0 : ntiles == 3 ? 1 : 2);
             int seg_count = 0;
+            const int seg_mask = (1 << P.seg_log2) - 1;
             uint32_t first = 0;   // 0: the next MMA of each tile overwrites its accumulator
             for (int c = 0; c < nch; ++c) {
                 const int s = c & 1;
@@ -558,7 +563,7 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
                 first = 1u;
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                              :: "r"(smem_u32(&bar_empty[s])) : "memory");
-                if ((c + 1) % SEG == 0 || c + 1 == nch) {
+                if (((c + 1) & seg_mask) == 0 || c + 1 == nch) {
                     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                                  :: "r"(smem_u32(&bar_seg)) : "memory");
                     if (!mbar_wait(smem_u32(&bar_drained), seg_count & 1)) { atomicExch(P.err, 4); abort_flag = 1; break; }
@@ -1212,7 +1217,8 @@ static EncodeTiledFn encode_tiled() {
 }
 
 int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_t* tri, const int32_t* tri_host,
-                     int ntri, double* bsum, void* ws, size_t ws_bytes, cudaStream_t st, bool run_plan) {
+                     int ntri, double* bsum, void* ws, size_t ws_bytes, cudaStream_t st, bool run_plan,
+                     bool fine_drain) {
     using namespace tc;
     PYSPEC_CHECK_ARG(tri_host != nullptr, "the BF16x3 contraction needs the host copy of the triangle list");
     PYSPEC_CHECK_ARG(nvox % 4 == 0, "BF16x3 contraction needs N^3 divisible by 4");
@@ -1275,6 +1281,7 @@ int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_
     P.slot_tri = d_stri;
     P.partials = partials;
     P.err = d_err;
+    P.seg_log2 = fine_drain ? SEG_LOG2_FINE : SEG_LOG2;
     PYSPEC_TRY(allow_smem((const void*)contract_tc_kernel, hp->smem));
     contract_tc_kernel<<<dim3(gx, P.ngroups), NTHREADS, hp->smem, st>>>(P, fmap);
     PYSPEC_LAUNCH_CHECK();

@@ -75,7 +75,7 @@ def _b0_from_half(half, alpha, I12, I13, I22, I23, I33, Nmax, Ncut, step, method
     plan.shells(half)
     plan.contract()
     bsum = plan.bsum.cpu().numpy()
-    if plan.method == "bf16x3":
+    if plan.method in core.TENSOR_METHODS:
         core.check_contract_status(plan.status_word().item())
     p0sum = plan.p0sum.cpu().numpy()
     V = float(n) ** 3

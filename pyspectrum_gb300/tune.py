@@ -227,15 +227,16 @@ def contract_flags(plan) -> int:
     """Method flags of the tuned tile plan for a BkPlan's triangle list
     (0: the default, pair cover where it needs fewer tiles; or
     CONTRACT_RUN_PLAN), timed on the plan's current fields the first time."""
-    if plan.method != "bf16x3" or not enabled():
+    from .core import METHODS, TENSOR_METHODS
+    if plan.method not in TENSOR_METHODS or not enabled():
         return 0
     digest = hashlib.sha1(plan.slots_host.tobytes()).hexdigest()[:16]
-    key = f"contract|{_device_key(plan.device)}|n{plan.n}|S{plan.S}|T{plan.T}|{digest}"
+    key = f"contract|{_device_key(plan.device)}|{plan.method}|n{plan.n}|S{plan.S}|T{plan.T}|{digest}"
     cands = [0, _lib.CONTRACT_RUN_PLAN]
 
     def run(flags):
         call("pyspec_bk_contract", ptr(plan.fields), plan.n, plan.S, ptr(plan.slots),
-             plan.slots_host.ctypes.data_as(ctypes.c_void_p), plan.T, _lib.CONTRACT_BF16X3 | flags,
+             plan.slots_host.ctypes.data_as(ctypes.c_void_p), plan.T, METHODS[plan.method] | flags,
              ptr(plan.bsum), ptr(plan.ws_con), plan.ws_con.numel(), stream_ptr())
     return int(_pick(key, cands, run))
 

@@ -158,11 +158,11 @@ def test_config2_all_triangles_fp64():
     assert tri.shape[1] == 6350
     bsum, absum, p0sum = _fp64_sums(half, step, jmin, nmax, tri)
     got = {}
-    for method in ("fp32", "bf16x3"):
+    for method in ("fp32", "bf16x3", "bf16x3_fine"):
         plan = core.get_plan(n, step, ncut, nmax, method)
         plan.run(half)
         got[method] = plan.bsum.cpu().numpy()
-        if method == "bf16x3":
+        if method in core.TENSOR_METHODS:
             core.check_contract_status(plan.status_word().item())
         rep = TF.error_report(got[method], bsum, absum)
         rep["p0_max_rel"] = float(np.max(np.abs(plan.p0sum.cpu().numpy() - p0sum) / p0sum))
@@ -178,13 +178,15 @@ def test_config2_all_triangles_fp64():
     _fresh()
     bsum_o, absum_o, _ = _fp64_sums(torch.from_numpy(hz), step, jmin, nmax, tri)
     del hz
-    for method in ("fp32", "bf16x3"):
+    for method in ("fp32", "bf16x3", "bf16x3_fine"):
         rep = TF.error_report(got[method], bsum_o, absum_o)
         rep.update(d_rep)
         _report(f"config2_end_to_end_{method}", rep)
     c2 = REPORT
     assert c2["config2_contraction_bf16x3"]["max_rel_cond_lt_1e3"] <= 1e-5
     assert c2["config2_contraction_bf16x3"]["normalised_max"] <= 2e-7
+    assert c2["config2_contraction_bf16x3_fine"]["max_rel_cond_lt_1e3"] <= 1e-5
+    assert c2["config2_contraction_bf16x3_fine"]["normalised_max"] <= 1e-7
     assert c2["config2_contraction_fp32"]["max_rel_cond_lt_1e3"] <= 1e-6
     assert c2["config2_contraction_fp32"]["normalised_max"] <= 1e-8
     assert c2["config2_contraction_fp32"]["p0_max_rel"] <= 1e-5
