@@ -558,7 +558,7 @@ def run_batch(args):
 def run_profile_delta(reps=3):
     """Profiling case for the delta(k) and P(k) kernels on the bench workload
     (1M particles, 360^3): `reps` rounds of clip/cast, the direct and the
-    8^3-tiled mass assignment, the 3D FFT (default radix plan), the
+    16^3-tiled mass assignment, the 3D FFT (default radix plan), the
     interlacing combine, the P(k) monopole and the pk_pbox_rsd multipoles.
     About 1.2 GB on the device; prints the last round's event times (not a
     bench result)."""
@@ -572,11 +572,11 @@ def run_profile_delta(reps=3):
     grid = torch.zeros((n, n, n), dtype=torch.complex64, device="cuda")
     half = torch.empty((n, n, n // 2 + 1), dtype=torch.complex64, device="cuda")
     kf_ks = float(np.float32(float(n) / L))
-    wst = torch.empty(_lib.load().pyspec_assign_tiled_workspace(npart, n, 8), dtype=torch.uint8, device="cuda")
+    wst = torch.empty(_lib.load().pyspec_assign_tiled_workspace(npart, n, 16), dtype=torch.uint8, device="cuda")
     nbin, nmu = n // 2, 10
     pko = torch.empty(6 * nbin, dtype=torch.float64, device="cuda")
     rso = torch.empty(2 * (5 * nbin + 4 * nbin * nmu), dtype=torch.float64, device="cuda")
-    names = ["prepare", "assign_direct", "assign_tiled8", "fft3d", "fcomb", "pk_mono", "pk_rsd"]
+    names = ["prepare", "assign_direct", "assign_tiled16", "fft3d", "fcomb", "pk_mono", "pk_rsd"]
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(names) + 1)]
     for _ in range(reps):
         ev[0].record()
@@ -586,7 +586,7 @@ def run_profile_delta(reps=3):
         call("pyspec_assign_pcs_interlaced", ptr(xyzs), ptr(ws), npart, n, kf_ks, 0.0, ptr(grid), stream_ptr())
         ev[2].record()
         grid.zero_()
-        call("pyspec_assign_pcs_interlaced_tiled", ptr(xyzs), ptr(ws), npart, n, kf_ks, 0.0, 8, ptr(grid),
+        call("pyspec_assign_pcs_interlaced_tiled", ptr(xyzs), ptr(ws), npart, n, kf_ks, 0.0, 16, ptr(grid),
              ptr(wst), wst.numel(), stream_ptr())
         ev[3].record()
         call("pyspec_fft3d_c2c", ptr(grid), n, 1, stream_ptr())

@@ -11,6 +11,12 @@ namespace pyspec {
 
 __device__ __forceinline__ int foldi(int i, int n) { return i <= n - i ? i : n - i; }
 
+// Each thread takes runs of kPkRun consecutive x of one row: along a row |k|
+// (and, mostly, mu) changes slowly, so the thread sums its modes of the same
+// bin in registers and adds each finished run to the shared histogram once,
+// instead of one shared-memory float64 atomic per mode and quantity.
+constexpr int kPkRun = 12;
+
 // Monopole on the reflected grid, summed over the half grid: planes x = 0 and
 // x = N/2 count once, others twice (k and -k); the seven Nyquist corners use
 // the real part only (pyspectrum.py:1149-1156).
@@ -24,19 +30,41 @@ __global__ void pk_mono_kernel(const float2* __restrict__ half, int n, double kf
     __syncthreads();
     const int z = blockIdx.x;
     const int zf = foldi(z, n);
-    for (int i = threadIdx.x; i < n * nh; i += blockDim.x) {
-        const int y = i / nh, x = i - y * nh;
+    const int nrun = (nh + kPkRun - 1) / kPkRun;
+    for (int item = threadIdx.x; item < n * nrun; item += blockDim.x) {
+        const int y = item / nrun, x0 = (item - y * nrun) * kPkRun, x1 = min(nh, x0 + kPkRun);
         const int yf = foldi(y, n);
-        const int64_t d2 = (int64_t)x * x + (int64_t)yf * yf + (int64_t)zf * zf;
-        const int b = shell_of(d2, 1);
-        if (b < 1 || b > nb) continue;
-        const float2 v = half[((int64_t)z * n + y) * nh + x];
-        const bool corner = (x == 0 || x == hg) && (y == 0 || y == hg) && (z == 0 || z == hg);
-        const float p = corner ? v.x * v.x : v.x * v.x + v.y * v.y;
-        const unsigned wgt = (x == 0 || x == hg) ? 1u : 2u;
-        atomicAdd(&ks[b - 1], (double)wgt * kf * (double)sqrtf((float)d2));
-        atomicAdd(&ps[b - 1], (double)wgt * (double)p);
-        atomicAdd(&cnt[b - 1], wgt);
+        const float2* row = half + ((int64_t)z * n + y) * nh;
+        int cb = -1;
+        double rk_s = 0.0, p_s = 0.0;
+        unsigned c_s = 0;
+        for (int x = x0; x < x1; ++x) {
+            const int64_t d2 = (int64_t)x * x + (int64_t)yf * yf + (int64_t)zf * zf;
+            const int b = shell_of(d2, 1);
+            if (b < 1 || b > nb) continue;
+            if (b != cb) {
+                if (cb >= 1) {
+                    atomicAdd(&ks[cb - 1], rk_s);
+                    atomicAdd(&ps[cb - 1], p_s);
+                    atomicAdd(&cnt[cb - 1], c_s);
+                }
+                cb = b;
+                rk_s = p_s = 0.0;
+                c_s = 0;
+            }
+            const float2 v = row[x];
+            const bool corner = (x == 0 || x == hg) && (y == 0 || y == hg) && (z == 0 || z == hg);
+            const float p = corner ? v.x * v.x : v.x * v.x + v.y * v.y;
+            const unsigned wgt = (x == 0 || x == hg) ? 1u : 2u;
+            rk_s += (double)wgt * kf * (double)sqrtf((float)d2);
+            p_s += (double)wgt * (double)p;
+            c_s += wgt;
+        }
+        if (cb >= 1) {
+            atomicAdd(&ks[cb - 1], rk_s);
+            atomicAdd(&ps[cb - 1], p_s);
+            atomicAdd(&cnt[cb - 1], c_s);
+        }
     }
     __syncthreads();
     for (int i = threadIdx.x; i < nb; i += blockDim.x) {
@@ -88,47 +116,83 @@ __global__ void pk_rsd_kernel(const float2* __restrict__ half, int n, int nbin, 
     const int fz = sfreq(iz);
     const int icz = (n - iz) % n;
     const double mub = (double)c.mubin;
-    for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
-        const int iy = i / n, ix = i - iy * n;
-        const int fy = sfreq(iy), fx = sfreq(ix);
-        const int64_t d2 = (int64_t)fx * fx + (int64_t)fy * fy + (int64_t)fz * fz;
-        const int imk = shell_of(d2, 1);
-        if (imk > nbin || imk == 0) continue;
-        const float rk = __fsqrt_rn((float)d2);
-        const float cot1 = __fdiv_rn((float)fz, rk);
-        const float sit1 = __fsqrt_rn(__fsub_rn(1.0f, __fmul_rn(cot1, cot1)));
-        float cc = 0.0f;
-        if (sit1 > 0.0f) {
-            const float rs = __fmul_rn(rk, sit1);
-            const float cp = __fdiv_rn((float)fx, rs);
-            const float sp = __fdiv_rn((float)fy, rs);
-            cc = __fadd_rn(__fmul_rn(c.sph, sp), __fmul_rn(c.cph, cp));
+    const int nrun = (n + kPkRun - 1) / kPkRun;
+    for (int item = threadIdx.x; item < n * nrun; item += blockDim.x) {
+        const int iy = item / nrun, x0 = (item - iy * nrun) * kPkRun, x1 = min(n, x0 + kPkRun);
+        const int fy = sfreq(iy);
+        const float2* row = half + ((int64_t)iz * n + iy) * nh;
+        const float2* mrow = half + ((int64_t)icz * n + (n - iy) % n) * nh;    // conjugate row
+        // running sums of the current k bin (cb) and (k, mu) cell (cm)
+        int cb = -1, cm = -1;
+        double s_n = 0, s_k = 0, s_p0 = 0, s_p2 = 0, s_p4 = 0;
+        double t_n = 0, t_k = 0, t_mu = 0, t_p = 0;
+        auto flush_b = [&]() {
+            if (cb < 0) return;
+            atomicAdd(&b_nk[cb], s_n);
+            atomicAdd(&b_k[cb], s_k);
+            atomicAdd(&b_p0[cb], s_p0);
+            atomicAdd(&b_p2[cb], s_p2);
+            atomicAdd(&b_p4[cb], s_p4);
+        };
+        auto flush_m = [&]() {
+            if (cm < 0) return;
+            atomicAdd(&m_n[cm], t_n);
+            atomicAdd(&m_k[cm], t_k);
+            atomicAdd(&m_mu[cm], t_mu);
+            atomicAdd(&m_p[cm], t_p);
+        };
+        for (int ix = x0; ix < x1; ++ix) {
+            const int fx = sfreq(ix);
+            const int64_t d2 = (int64_t)fx * fx + (int64_t)fy * fy + (int64_t)fz * fz;
+            const int imk = shell_of(d2, 1);
+            if (imk > nbin || imk == 0) continue;
+            const float rk = __fsqrt_rn((float)d2);
+            const float cot1 = __fdiv_rn((float)fz, rk);
+            const float sit1 = __fsqrt_rn(__fsub_rn(1.0f, __fmul_rn(cot1, cot1)));
+            float cc = 0.0f;
+            if (sit1 > 0.0f) {
+                const float rs = __fmul_rn(rk, sit1);
+                const float cp = __fdiv_rn((float)fx, rs);
+                const float sp = __fdiv_rn((float)fy, rs);
+                cc = __fadd_rn(__fmul_rn(c.sph, sp), __fmul_rn(c.cph, cp));
+            }
+            // mu: single-precision expression stored in real*8 (estimator.f:218)
+            const double mu = (double)__fadd_rn(__fmul_rn(c.ct, cot1), __fmul_rn(__fmul_rn(c.st, sit1), cc));
+            const int imu = (int)((fabs(mu) + mub) / mub);
+            // Legendre factors in real*8 (estimator.f:221-222)
+            const double mu2 = __dmul_rn(mu, mu);
+            const double le2 = __dadd_rn(-0.5, __dmul_rn(1.5, mu2));
+            const double le4 = __dadd_rn(__dsub_rn(0.375, __dmul_rn(3.75, mu2)), __dmul_rn(4.375, __dmul_rn(mu2, mu2)));
+            const float2 ct = ix <= n / 2 ? row[ix] : mrow[(n - ix) % n];
+            const float am = hypotf(ct.x, ct.y);              // cabs(ct), single precision
+            const double pkd = (double)__fmul_rn(am, am);     // pk = cabs(ct)**2 (estimator.f:230)
+            const double kv = (double)__fmul_rn(c.kf, rk);    // dble(kf*rk)
+            const int b = imk - 1;
+            if (b != cb) {
+                flush_b();
+                cb = b;
+                s_n = s_k = s_p0 = s_p2 = s_p4 = 0.0;
+            }
+            s_n += 1.0;
+            s_k += kv;
+            s_p0 += pkd;
+            s_p2 += __dmul_rn(__dmul_rn(pkd, 5.0), le2);       // dble(pk)*5.d0*Le2
+            s_p4 += __dmul_rn(__dmul_rn(pkd, 9.0), le4);
+            if (imu <= nmu && imu > 0) {
+                const int m = b * nmu + imu - 1;
+                if (m != cm) {
+                    flush_m();
+                    cm = m;
+                    t_n = t_k = t_mu = t_p = 0.0;
+                }
+                t_n += 1.0;
+                t_k += kv;
+                t_mu += fabs(mu);
+                t_p += pkd;
+            }
         }
-        const float muf = __fadd_rn(__fmul_rn(c.ct, cot1), __fmul_rn(__fmul_rn(c.st, sit1), cc));
-        const double mu = (double)muf;
-        const int imu = (int)((fabs(mu) + mub) / mub);
-        float2 ct;
-        if (ix <= n / 2) ct = half[((int64_t)iz * n + iy) * nh + ix];
-        else ct = half[((int64_t)icz * n + (n - iy) % n) * nh + (n - ix) % n];
-        const float pk = ct.x * ct.x + ct.y * ct.y;
-        const float mu2 = muf * muf;
-        const float le2 = -0.5f + 1.5f * mu2;
-        const float le4 = 0.375f - 3.75f * mu2 + 4.375f * mu2 * mu2;
-        const double kv = (double)__fmul_rn(c.kf, rk);
-        const double pkd = (double)pk;
-        const int b = imk - 1;
-        atomicAdd(&b_nk[b], 1.0);
-        atomicAdd(&b_k[b], kv);
-        atomicAdd(&b_p0[b], pkd);
-        atomicAdd(&b_p2[b], (double)(pk * 5.0f * le2));
-        atomicAdd(&b_p4[b], (double)(pk * 9.0f * le4));
-        if (imu <= nmu && imu > 0) {
-            const int m = b * nmu + imu - 1;
-            atomicAdd(&m_n[m], 1.0);
-            atomicAdd(&m_k[m], kv);
-            atomicAdd(&m_mu[m], fabs(mu));
-            atomicAdd(&m_p[m], pkd);
-        }
+        flush_b();
+        flush_m();
     }
     __syncthreads();
     for (int i = threadIdx.x; i < tot; i += blockDim.x)

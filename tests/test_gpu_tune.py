@@ -72,7 +72,7 @@ def test_tiled_assignment_matches_direct_and_oracle(n, L, offset_cells, clustere
         # the cells touched are exactly the same
         np.testing.assert_array_equal(got != 0, ref != 0, err_msg=kind)
     # mass: every particle deposits its weight (x 6^3 per grid) on both grids
-    tot = ref.sum(axis=(0, 1, 2)) / 216.0
+    tot = ref.astype(np.float64).sum(axis=(0, 1, 2)) / 216.0
     wsum = npart if w is None else float(np.sum(w.astype(np.float32)))
     np.testing.assert_allclose(tot, [wsum, wsum], rtol=1e-5)
 
@@ -170,7 +170,8 @@ def test_tuner_caches_choices(tmp_path, monkeypatch):
     kinds = sorted(k.split("|")[0] for k in saved)
     assert kinds == ["assign", "fft3d"]
     for k, v in saved.items():
-        assert len(v["ms"]) >= 2 and str(v["choice"]) in v["ms"]
+        # 64^3 has one FFT form (Stockham); the assignment has four candidates
+        assert len(v["ms"]) >= (4 if k.startswith("assign") else 1) and str(v["choice"]) in v["ms"]
     # a second call reuses the choices (no new keys) and gives the same delta(k)
     h2 = core.fft_periodic_half(xyzs, ws, n, L, 300_000.0)
     with open(tmp_path / "tune.json") as f:
