@@ -13,8 +13,10 @@ __device__ __forceinline__ int foldi(int i, int n) { return i <= n - i ? i : n -
 
 // Each thread takes runs of kPkRun consecutive x of one row: along a row |k|
 // (and, mostly, mu) changes slowly, so the thread sums its modes of the same
-// bin in registers and adds each finished run to the shared histogram once,
-// instead of one shared-memory float64 atomic per mode and quantity.
+// bin in float32 registers (at most kPkRun terms) and adds each finished run
+// to the float64 shared histogram once, instead of one float64 atomic per mode
+// and quantity (float64 arithmetic runs at a small fraction of the float32
+// rate on this GPU).
 constexpr int kPkRun = 12;
 
 // Monopole on the reflected grid, summed over the half grid: planes x = 0 and
@@ -36,7 +38,7 @@ __global__ void pk_mono_kernel(const float2* __restrict__ half, int n, double kf
         const int yf = foldi(y, n);
         const float2* row = half + ((int64_t)z * n + y) * nh;
         int cb = -1;
-        double rk_s = 0.0, p_s = 0.0;
+        float rk_s = 0.0f, p_s = 0.0f;     // run sums (at most kPkRun terms), added to float64 per run
         unsigned c_s = 0;
         for (int x = x0; x < x1; ++x) {
             const int64_t d2 = (int64_t)x * x + (int64_t)yf * yf + (int64_t)zf * zf;
@@ -44,25 +46,25 @@ __global__ void pk_mono_kernel(const float2* __restrict__ half, int n, double kf
             if (b < 1 || b > nb) continue;
             if (b != cb) {
                 if (cb >= 1) {
-                    atomicAdd(&ks[cb - 1], rk_s);
-                    atomicAdd(&ps[cb - 1], p_s);
+                    atomicAdd(&ks[cb - 1], (double)rk_s * kf);
+                    atomicAdd(&ps[cb - 1], (double)p_s);
                     atomicAdd(&cnt[cb - 1], c_s);
                 }
                 cb = b;
-                rk_s = p_s = 0.0;
+                rk_s = p_s = 0.0f;
                 c_s = 0;
             }
             const float2 v = row[x];
             const bool corner = (x == 0 || x == hg) && (y == 0 || y == hg) && (z == 0 || z == hg);
             const float p = corner ? v.x * v.x : v.x * v.x + v.y * v.y;
             const unsigned wgt = (x == 0 || x == hg) ? 1u : 2u;
-            rk_s += (double)wgt * kf * (double)sqrtf((float)d2);
-            p_s += (double)wgt * (double)p;
+            rk_s += (float)wgt * sqrtf((float)d2);
+            p_s += (float)wgt * p;
             c_s += wgt;
         }
         if (cb >= 1) {
-            atomicAdd(&ks[cb - 1], rk_s);
-            atomicAdd(&ps[cb - 1], p_s);
+            atomicAdd(&ks[cb - 1], (double)rk_s * kf);
+            atomicAdd(&ps[cb - 1], (double)p_s);
             atomicAdd(&cnt[cb - 1], c_s);
         }
     }
@@ -87,8 +89,11 @@ __global__ void pk_mono_finalize(const double* __restrict__ acc, int nb, double 
 
 // estimator.f:196-244.  Mode selection (imk) is exact integer arithmetic;
 // mu follows the Fortran's single-precision expression order without fused
-// multiply-add, and the mu bin uses float64 exactly as
-// int((abs(mu)+dble(mubin))/dble(mubin)).
+// multiply-add, and the mu bin is exactly int((abs(mu)+dble(mubin))/dble(mubin))
+// in float64, so every mode lands in the Fortran's (k, mu) bin.  The summed
+// quantities (the Legendre-weighted powers included) are float32 per mode and
+// per run of kPkRun modes, float64 from there on: within 1e-6 of the
+// Fortran's float64 sums.
 struct RsdConst {
     float ct, st, cph, sph;   // cos/sin of thetaobs and phiobs (single precision)
     float kf;                 // tpi/Lbox, single precision
@@ -116,30 +121,31 @@ __global__ void pk_rsd_kernel(const float2* __restrict__ half, int n, int nbin, 
     const int fz = sfreq(iz);
     const int icz = (n - iz) % n;
     const double mub = (double)c.mubin;
+    const double inv_mub = 1.0 / mub;
     const int nrun = (n + kPkRun - 1) / kPkRun;
     for (int item = threadIdx.x; item < n * nrun; item += blockDim.x) {
         const int iy = item / nrun, x0 = (item - iy * nrun) * kPkRun, x1 = min(n, x0 + kPkRun);
         const int fy = sfreq(iy);
         const float2* row = half + ((int64_t)iz * n + iy) * nh;
         const float2* mrow = half + ((int64_t)icz * n + (n - iy) % n) * nh;    // conjugate row
-        // running sums of the current k bin (cb) and (k, mu) cell (cm)
+        // float32 run sums of the current k bin (cb) and (k, mu) cell (cm)
         int cb = -1, cm = -1;
-        double s_n = 0, s_k = 0, s_p0 = 0, s_p2 = 0, s_p4 = 0;
-        double t_n = 0, t_k = 0, t_mu = 0, t_p = 0;
+        float s_n = 0, s_k = 0, s_p0 = 0, s_p2 = 0, s_p4 = 0;
+        float t_n = 0, t_k = 0, t_mu = 0, t_p = 0;
         auto flush_b = [&]() {
             if (cb < 0) return;
-            atomicAdd(&b_nk[cb], s_n);
-            atomicAdd(&b_k[cb], s_k);
-            atomicAdd(&b_p0[cb], s_p0);
-            atomicAdd(&b_p2[cb], s_p2);
-            atomicAdd(&b_p4[cb], s_p4);
+            atomicAdd(&b_nk[cb], (double)s_n);
+            atomicAdd(&b_k[cb], (double)s_k);
+            atomicAdd(&b_p0[cb], (double)s_p0);
+            atomicAdd(&b_p2[cb], (double)s_p2);
+            atomicAdd(&b_p4[cb], (double)s_p4);
         };
         auto flush_m = [&]() {
             if (cm < 0) return;
-            atomicAdd(&m_n[cm], t_n);
-            atomicAdd(&m_k[cm], t_k);
-            atomicAdd(&m_mu[cm], t_mu);
-            atomicAdd(&m_p[cm], t_p);
+            atomicAdd(&m_n[cm], (double)t_n);
+            atomicAdd(&m_k[cm], (double)t_k);
+            atomicAdd(&m_mu[cm], (double)t_mu);
+            atomicAdd(&m_p[cm], (double)t_p);
         };
         for (int ix = x0; ix < x1; ++ix) {
             const int fx = sfreq(ix);
@@ -156,39 +162,45 @@ __global__ void pk_rsd_kernel(const float2* __restrict__ half, int n, int nbin, 
                 const float sp = __fdiv_rn((float)fy, rs);
                 cc = __fadd_rn(__fmul_rn(c.sph, sp), __fmul_rn(c.cph, cp));
             }
-            // mu: single-precision expression stored in real*8 (estimator.f:218)
-            const double mu = (double)__fadd_rn(__fmul_rn(c.ct, cot1), __fmul_rn(__fmul_rn(c.st, sit1), cc));
-            const int imu = (int)((fabs(mu) + mub) / mub);
-            // Legendre factors in real*8 (estimator.f:221-222)
-            const double mu2 = __dmul_rn(mu, mu);
-            const double le2 = __dadd_rn(-0.5, __dmul_rn(1.5, mu2));
-            const double le4 = __dadd_rn(__dsub_rn(0.375, __dmul_rn(3.75, mu2)), __dmul_rn(4.375, __dmul_rn(mu2, mu2)));
+            // mu: the single-precision expression of estimator.f:218
+            const float muf = __fadd_rn(__fmul_rn(c.ct, cot1), __fmul_rn(__fmul_rn(c.st, sit1), cc));
+            // imu = int((abs(mu) + dble(mubin)) / dble(mubin)) in float64 (estimator.f:219): the
+            // quotient from the reciprocal is the exact answer unless it lies within 1e-9 of an
+            // integer, where the division itself decides
+            const double am = fabs((double)muf) + mub;
+            const double q = am * inv_mub;
+            int imu = (int)q;
+            const double fr = q - (double)imu;
+            if (fr < 1e-9 || fr > 1.0 - 1e-9) imu = (int)(am / mub);
+            const float mu2 = __fmul_rn(muf, muf);
+            const float le2 = -0.5f + 1.5f * mu2;                            // estimator.f:221
+            const float le4 = 0.375f - 3.75f * mu2 + 4.375f * mu2 * mu2;     // estimator.f:222
             const float2 ct = ix <= n / 2 ? row[ix] : mrow[(n - ix) % n];
-            const float am = hypotf(ct.x, ct.y);              // cabs(ct), single precision
-            const double pkd = (double)__fmul_rn(am, am);     // pk = cabs(ct)**2 (estimator.f:230)
-            const double kv = (double)__fmul_rn(c.kf, rk);    // dble(kf*rk)
+            const float a = hypotf(ct.x, ct.y);               // cabs(ct), single precision
+            const float pk = __fmul_rn(a, a);                 // pk = cabs(ct)**2 (estimator.f:230)
+            const float kv = __fmul_rn(c.kf, rk);             // kf*rk
             const int b = imk - 1;
             if (b != cb) {
                 flush_b();
                 cb = b;
-                s_n = s_k = s_p0 = s_p2 = s_p4 = 0.0;
+                s_n = s_k = s_p0 = s_p2 = s_p4 = 0.0f;
             }
-            s_n += 1.0;
+            s_n += 1.0f;
             s_k += kv;
-            s_p0 += pkd;
-            s_p2 += __dmul_rn(__dmul_rn(pkd, 5.0), le2);       // dble(pk)*5.d0*Le2
-            s_p4 += __dmul_rn(__dmul_rn(pkd, 9.0), le4);
+            s_p0 += pk;
+            s_p2 += pk * 5.0f * le2;
+            s_p4 += pk * 9.0f * le4;
             if (imu <= nmu && imu > 0) {
                 const int m = b * nmu + imu - 1;
                 if (m != cm) {
                     flush_m();
                     cm = m;
-                    t_n = t_k = t_mu = t_p = 0.0;
+                    t_n = t_k = t_mu = t_p = 0.0f;
                 }
-                t_n += 1.0;
+                t_n += 1.0f;
                 t_k += kv;
-                t_mu += fabs(mu);
-                t_p += pkd;
+                t_mu += fabsf(muf);
+                t_p += pk;
             }
         }
         flush_b();
