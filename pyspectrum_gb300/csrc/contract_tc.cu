@@ -485,12 +485,14 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
             // A operand: this thread's 8 (or 4) pair rows x 4 voxels of its k-step, straight into TMEM
             if (tp_on) {
                 const float4 fi0 = lds4(F, oi0);
+                // the second slot's pair shell is loaded before the first slot's
+                // TMEM stores, which the compiler may not move loads across
+                const float4 fi1 = slot1_on ? lds4(F, oi1) : fi0;
                 float4 fj[4];
 #pragma unroll
                 for (int y = 0; y < 4; ++y) fj[y] = lds4(F, oj0[y]);
                 store_slot(fi0, fj, lane_base + acol(s, 2 * tp, kstep));
                 if (slot1_on) {
-                    const float4 fi1 = lds4(F, oi1);
                     if (reload) {
 #pragma unroll
                         for (int y = 0; y < 4; ++y) fj[y] = lds4(F, foff((int)((gs1 >> (8 * y)) & 0xffu)));

@@ -18,6 +18,26 @@ template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
     C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
 }
 template <typename C, typename T> __device__ __forceinline__ C cscale(C a, T s) { C r; r.x = a.x * s; r.y = a.y * s; return r; }
+// complex64 add, subtract and scale as packed two-lane FP32 instructions
+// (add/sub/mul.rn.f32x2, sm_100+): one instruction per complex operation,
+// same rounding as the two scalar ones.  The templates above serve complex128.
+__device__ __forceinline__ unsigned long long pk_u64(float2 a) { return *reinterpret_cast<unsigned long long*>(&a); }
+__device__ __forceinline__ float2 pk_f2(unsigned long long u) { return *reinterpret_cast<float2*>(&u); }
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pk_u64(a)), "l"(pk_u64(b)));
+    return pk_f2(r);
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pk_u64(a)), "l"(pk_u64(b)));
+    return pk_f2(r);
+}
+__device__ __forceinline__ float2 cscale(float2 a, float s) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pk_u64(a)), "l"(pk_u64(make_float2(s, s))));
+    return pk_f2(r);
+}
 // multiply by sign*i
 template <typename C> __device__ __forceinline__ C cmul_si(C a, int sign) {
     C r;

@@ -121,7 +121,7 @@ __global__ void pk_rsd_kernel(const float2* __restrict__ half, int n, int nbin, 
     const int fz = sfreq(iz);
     const int icz = (n - iz) % n;
     const double mub = (double)c.mubin;
-    const double inv_mub = 1.0 / mub;
+    const float inv_mubf = 1.0f / c.mubin;
     const int nrun = (n + kPkRun - 1) / kPkRun;
     for (int item = threadIdx.x; item < n * nrun; item += blockDim.x) {
         const int iy = item / nrun, x0 = (item - iy * nrun) * kPkRun, x1 = min(n, x0 + kPkRun);
@@ -164,14 +164,14 @@ __global__ void pk_rsd_kernel(const float2* __restrict__ half, int n, int nbin, 
             }
             // mu: the single-precision expression of estimator.f:218
             const float muf = __fadd_rn(__fmul_rn(c.ct, cot1), __fmul_rn(__fmul_rn(c.st, sit1), cc));
-            // imu = int((abs(mu) + dble(mubin)) / dble(mubin)) in float64 (estimator.f:219): the
-            // quotient from the reciprocal is the exact answer unless it lies within 1e-9 of an
-            // integer, where the division itself decides
-            const double am = fabs((double)muf) + mub;
-            const double q = am * inv_mub;
-            int imu = (int)q;
-            const double fr = q - (double)imu;
-            if (fr < 1e-9 || fr > 1.0 - 1e-9) imu = (int)(am / mub);
+            // imu = int((abs(mu) + dble(mubin)) / dble(mubin)) in float64 (estimator.f:219).  The
+            // float32 quotient is within 2e-6 of it, so its integer part is the answer unless it
+            // lies within 1e-4 of an integer; there the float64 division decides (float64 runs
+            // at a small fraction of the float32 rate on this GPU)
+            const float qf = (fabsf(muf) + c.mubin) * inv_mubf;
+            int imu = (int)qf;
+            const float ff = qf - (float)imu;
+            if (ff < 1e-4f || ff > 1.0f - 1e-4f) imu = (int)((fabs((double)muf) + mub) / mub);
             const float mu2 = __fmul_rn(muf, muf);
             const float le2 = -0.5f + 1.5f * mu2;                            // estimator.f:221
             const float le4 = 0.375f - 3.75f * mu2 + 4.375f * mu2 * mu2;     // estimator.f:222
