@@ -345,7 +345,7 @@ def run_gpu(args, rank, world, local_rank):
     grid = torch.zeros((n, n, n), dtype=torch.complex64, device=dev)
     half = torch.empty((n, n, n // 2 + 1), dtype=torch.complex64, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
-    plans = {m: core.get_plan(n, step, ncut, nmax, m, dev) for m in ("bf16x3", "fp32", "bf16x3_fine")}
+    plans = {m: core.get_plan(n, step, ncut, nmax, m, dev) for m in ("bf16x3", "fp32", "bf16x3_fine", "bf16x6")}
 
     def step_fn(plan, ev=None):
         if ev is not None:
@@ -369,7 +369,7 @@ def run_gpu(args, rank, world, local_rank):
             dist.barrier()
 
     results = {}
-    for method in ("bf16x3", "fp32", "bf16x3_fine"):
+    for method in ("bf16x3", "fp32", "bf16x3_fine", "bf16x6"):
         plan = plans[method]
         steps = args.steps if method == "bf16x3" else max(1, min(args.steps, 5))
         for _ in range(args.warmup):

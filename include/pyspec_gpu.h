@@ -48,11 +48,16 @@ extern "C" {
 /* Contraction methods for pyspec_bk_contract. */
 #define PYSPEC_CONTRACT_FP32 0    /* FP32 CUDA-core, FP32 per-thread, FP64 across blocks */
 #define PYSPEC_CONTRACT_BF16X3 1  /* tcgen05 tensor cores, hi+lo BF16 split, 3 products */
-/* Flag OR-ed into the BF16X3 method: plan the tensor-core tiles from runs of
+/* tcgen05 tensor cores, 6 products: the BF16X3 sums (drained every 8 chunks)
+ * plus a second pass over the voxels with each operand's third bf16 part
+ * (x = hi + lo + res): sum P_res F_hi + P_hi F_res.  About twice the BF16X3
+ * time, for errors near the FP32 form's. */
+#define PYSPEC_CONTRACT_BF16X6 2
+/* Flag OR-ed into a tensor-core method: plan the tensor-core tiles from runs of
  * each triangle's two largest shells even where a pair cover would need
  * fewer tiles (same sums; for the autotuner, which times both plans). */
 #define PYSPEC_CONTRACT_RUN_PLAN 0x100
-/* Flag OR-ed into the BF16X3 method: drain the tensor-memory FP32
+/* Flag OR-ed into a tensor-core method: drain the tensor-memory FP32
  * accumulators into the compensated sums every 8 chunks of 32 voxels instead
  * of every 32.  The split-BF16 error is set by the length of that FP32
  * accumulation, so this trades drain time for about 4x smaller errors. */

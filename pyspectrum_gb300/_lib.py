@@ -58,6 +58,7 @@ SIGNATURES = {
 
 CONTRACT_FP32 = 0
 CONTRACT_BF16X3 = 1
+CONTRACT_BF16X6 = 2
 CONTRACT_RUN_PLAN = 0x100
 CONTRACT_FINE_DRAIN = 0x200
 

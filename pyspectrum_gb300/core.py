@@ -26,10 +26,11 @@ from ._lib import call, ptr, stream_ptr
 
 # contraction methods: FP32 CUDA cores; split-BF16 tensor cores with the
 # accumulators drained every 32 chunks ('bf16x3') or every 8 ('bf16x3_fine':
-# about 4x smaller error, the drains cost more time)
+# about 4x smaller error, the drains cost more time); and 'bf16x6', which adds
+# a second tensor-core pass with the operands' third bf16 parts (6 products)
 METHODS = {"fp32": _lib.CONTRACT_FP32, "bf16x3": _lib.CONTRACT_BF16X3,
-           "bf16x3_fine": _lib.CONTRACT_BF16X3 | _lib.CONTRACT_FINE_DRAIN}
-TENSOR_METHODS = ("bf16x3", "bf16x3_fine")
+           "bf16x3_fine": _lib.CONTRACT_BF16X3 | _lib.CONTRACT_FINE_DRAIN, "bf16x6": _lib.CONTRACT_BF16X6}
+TENSOR_METHODS = ("bf16x3", "bf16x3_fine", "bf16x6")
 
 
 def _dev(device=None) -> torch.device:

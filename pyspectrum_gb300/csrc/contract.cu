@@ -645,6 +645,7 @@ extern "C" size_t pyspec_bk_contract_workspace(int ngrid, int nshell, int ntri, 
     if (ngrid < 2 || nshell < 1 || ntri < 0) return 0;
     const int64_t V = (int64_t)ngrid * ngrid * ngrid;
     if (method == PYSPEC_CONTRACT_BF16X3) return contract_tc_ws(V, nshell, ntri);
+    if (method == PYSPEC_CONTRACT_BF16X6) return contract_tc_ws(V, nshell, ntri, true);
     return std::max(contract_fp32_ws(V, nshell, ntri), contract_simple_ws(V, ntri));
 }
 
@@ -664,8 +665,9 @@ extern "C" int pyspec_bk_contract(const float* fields, int ngrid, int nshell, co
     const bool run_plan = (method & PYSPEC_CONTRACT_RUN_PLAN) != 0;
     const bool fine_drain = (method & PYSPEC_CONTRACT_FINE_DRAIN) != 0;
     method &= ~(PYSPEC_CONTRACT_RUN_PLAN | PYSPEC_CONTRACT_FINE_DRAIN);
-    PYSPEC_CHECK_ARG((!run_plan && !fine_drain) || method == PYSPEC_CONTRACT_BF16X3,
-                     "PYSPEC_CONTRACT_RUN_PLAN and PYSPEC_CONTRACT_FINE_DRAIN apply to BF16X3 only");
+    PYSPEC_CHECK_ARG((!run_plan && !fine_drain) || method == PYSPEC_CONTRACT_BF16X3 ||
+                         method == PYSPEC_CONTRACT_BF16X6,
+                     "PYSPEC_CONTRACT_RUN_PLAN and PYSPEC_CONTRACT_FINE_DRAIN apply to the tensor-core methods only");
     if (method == PYSPEC_CONTRACT_FP32) {
         if (tri_host == nullptr)   // device-only triangle list: the unplanned kernel
             return contract_simple_impl<float>(fields, V, nshell, tri, ntri, nullptr, V, bsum,
@@ -675,6 +677,9 @@ extern "C" int pyspec_bk_contract(const float* fields, int ngrid, int nshell, co
     if (method == PYSPEC_CONTRACT_BF16X3)
         return contract_tc_impl(fields, V, nshell, tri, tri_host, ntri, bsum, workspace, ws_bytes, st, run_plan,
                                 fine_drain);
+    if (method == PYSPEC_CONTRACT_BF16X6)
+        return contract_tc_impl(fields, V, nshell, tri, tri_host, ntri, bsum, workspace, ws_bytes, st, run_plan,
+                                true, true);
     set_error("unknown contraction method %d", method);
     return PYSPEC_E_INVALID;
 }

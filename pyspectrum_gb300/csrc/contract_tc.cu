@@ -115,6 +115,7 @@ struct Params {
     double* partials;            // [gridDim.x][ntri]
     int* err;
     int seg_log2;                // accumulators drained every 2^seg_log2 chunks
+    int residual;                // 1: the residual pass of the 6-product form (see contract_tc_impl)
     int ngroups;
     int maxslots;
     Group g[MAXGROUPS];
@@ -249,6 +250,26 @@ __device__ __forceinline__ void split2(float2 p, uint32_t& h, uint32_t& l) {
     l = pack_bf16x2(lv.x, lv.y);
 }
 
+// hi and third parts of two floats, for the residual pass: x = hi + lo + res
+// with hi = bf16(x), lo = bf16(x - hi), res = bf16(x - hi - lo); both
+// differences are exact in float32, so hi + lo + res carries ~24 bits.
+__device__ __forceinline__ void split2_res(float2 p, uint32_t& h, uint32_t& r) {
+    h = pack_bf16x2(p.x, p.y);
+    const float2 lv = sub2(p, make_float2(__uint_as_float(h << 16), __uint_as_float(h & 0xFFFF0000u)));
+    const uint32_t l = pack_bf16x2(lv.x, lv.y);
+    const float2 rv = sub2(lv, make_float2(__uint_as_float(l << 16), __uint_as_float(l & 0xFFFF0000u)));
+    r = pack_bf16x2(rv.x, rv.y);
+}
+
+// split_store8 for the residual pass: the hi part and the third part.
+__device__ __forceinline__ void split_store8_res(const float2* x, char* hi, char* res) {
+    uint32_t h[4], r[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) split2_res(x[q], h[q], r[q]);
+    *reinterpret_cast<uint4*>(hi) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4*>(res) = make_uint4(r[0], r[1], r[2], r[3]);
+}
+
 // One slot of a producer thread into TMEM for its k-step: the products
 // fi * fj[y] (4 voxels each) of its four pair rows y = 0..3, which sit at
 // lanes x + 8y of the lane quarter (`addr` = quarter base + the tile's A
@@ -256,6 +277,8 @@ __device__ __forceinline__ void split2(float2 p, uint32_t& h, uint32_t& l) {
 // to the 16-lane block [0, 16), rows 2, 3 to [16, 32); repeat 0 of the x2
 // shape carries the hi parts, repeat 1 the lo parts; lane a of the thread
 // group owns columns 2a, 2a + 1 of each repeat (voxels 4a .. 4a + 3).
+// RES (the residual pass): the lo columns receive the third part instead.
+template <bool RES = false>
 __device__ __forceinline__ void store_slot(float4 fi, const float4* fj, uint32_t addr) {
 #pragma unroll
     for (int blk = 0; blk < 2; ++blk) {
@@ -263,8 +286,15 @@ __device__ __forceinline__ void store_slot(float4 fi, const float4* fj, uint32_t
 #pragma unroll
         for (int yy = 0; yy < 2; ++yy) {
             const float4 f = fj[2 * blk + yy];
-            split2(mul2(make_float2(fi.x, fi.y), make_float2(f.x, f.y)), v[2 * yy], v[4 + 2 * yy]);
-            split2(mul2(make_float2(fi.z, fi.w), make_float2(f.z, f.w)), v[2 * yy + 1], v[4 + 2 * yy + 1]);
+            const float2 p0 = mul2(make_float2(fi.x, fi.y), make_float2(f.x, f.y));
+            const float2 p1 = mul2(make_float2(fi.z, fi.w), make_float2(f.z, f.w));
+            if constexpr (RES) {
+                split2_res(p0, v[2 * yy], v[4 + 2 * yy]);
+                split2_res(p1, v[2 * yy + 1], v[4 + 2 * yy + 1]);
+            } else {
+                split2(p0, v[2 * yy], v[4 + 2 * yy]);
+                split2(p1, v[2 * yy + 1], v[4 + 2 * yy + 1]);
+            }
         }
         tmem_st16x256_x2(addr + ((uint32_t)(16 * blk) << 16), v);
     }
@@ -276,9 +306,12 @@ __device__ __forceinline__ void store_slot(float4 fi, const float4* fj, uint32_t
 // of the stage's A columns (tile t, k-step ks at + 32 t + 16 ks), `bd0` = the
 // stage's B descriptor (k-step ks at + 256 bytes).  `first` == 0 starts each
 // accumulator afresh.
-template <bool WIDE, int NT>
+// RES (the residual pass, narrow form only): A_res (held in the lo columns)
+// against B_hi, then A_hi against B_res (held in the B lo rows).
+template <bool WIDE, int NT, bool RES = false>
 __device__ __forceinline__ void issue_chunk(const uint32_t (&dcol)[MAXTILES], uint32_t abase, uint64_t bd0,
                                             const uint32_t (&idesc)[MAXTILES], uint32_t first) {
+    static_assert(!(RES && WIDE), "the residual pass uses the narrow form");
 #pragma unroll
     for (int ks = 0; ks < KC / 16; ++ks) {
         const uint32_t acc0 = ks == 0 ? first : 1u;
@@ -286,6 +319,13 @@ __device__ __forceinline__ void issue_chunk(const uint32_t (&dcol)[MAXTILES], ui
 #pragma unroll
         for (int t = 0; t < NT; ++t) {
             const uint32_t ahi = abase + (uint32_t)(t * ACOLS + ks * 16);
+            if constexpr (RES) {
+                asm volatile("{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n"
+                             :: "r"(dcol[t]), "r"(ahi + 8u), "l"(bd), "r"(idesc[t]), "r"(acc0));
+                asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, 1;"
+                             :: "r"(dcol[t]), "r"(ahi), "l"(bd + (uint64_t)(512 >> 4)), "r"(idesc[t]));
+                continue;
+            }
             asm volatile("{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n"
                          :: "r"(dcol[t]), "r"(ahi), "l"(bd), "r"(idesc[t]), "r"(acc0));
             asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, 1;"
@@ -480,7 +520,8 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
                 const float4 e = *reinterpret_cast<const float4*>(F + fchunk(ub_r, 2 * ub_g + 1));
                 const float2 x[4] = {make_float2(a.x, a.y), make_float2(a.z, a.w), make_float2(e.x, e.y),
                                      make_float2(e.z, e.w)};
-                split_store8(x, Bst + op_off(brow(ub_r, 0), ub_g), Bst + op_off(brow(ub_r, 1), ub_g));
+                if (P.residual) split_store8_res(x, Bst + op_off(brow(ub_r, 0), ub_g), Bst + op_off(brow(ub_r, 1), ub_g));
+                else split_store8(x, Bst + op_off(brow(ub_r, 0), ub_g), Bst + op_off(brow(ub_r, 1), ub_g));
             }
             // A operand: this thread's 8 (or 4) pair rows x 4 voxels of its k-step, straight into TMEM
             if (tp_on) {
@@ -491,13 +532,15 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
                 float4 fj[4];
 #pragma unroll
                 for (int y = 0; y < 4; ++y) fj[y] = lds4(F, oj0[y]);
-                store_slot(fi0, fj, lane_base + acol(s, 2 * tp, kstep));
+                if (P.residual) store_slot<true>(fi0, fj, lane_base + acol(s, 2 * tp, kstep));
+                else store_slot(fi0, fj, lane_base + acol(s, 2 * tp, kstep));
                 if (slot1_on) {
                     if (reload) {
 #pragma unroll
                         for (int y = 0; y < 4; ++y) fj[y] = lds4(F, foff((int)((gs1 >> (8 * y)) & 0xffu)));
                     }
-                    store_slot(fi1, fj, lane_base + acol(s, 2 * tp + 1, kstep));
+                    if (P.residual) store_slot<true>(fi1, fj, lane_base + acol(s, 2 * tp + 1, kstep));
+                    else store_slot(fi1, fj, lane_base + acol(s, 2 * tp + 1, kstep));
                 }
             }
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
@@ -542,7 +585,7 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
             // apart; the lo blocks are 512 bytes further)
             const uint64_t bdesc0 = make_desc(sbase, 128, wide ? 512 : 1024);
             // tile count 2, 3 or 4 and the form select one branch-free sequence
-            const int mode = (wide ? 3 : 0) + (ntiles == 2 ? 0 : ntiles == 3 ? 1 : 2);
+            const int mode = (P.residual ? 6 : wide ? 3 : 0) + (ntiles == 2 ? 0 : ntiles == 3 ? 1 : 2);
             int seg_count = 0;
             const int seg_mask = (1 << P.seg_log2) - 1;
             uint32_t first = 0;   // 0: the next MMA of each tile overwrites its accumulator
@@ -560,7 +603,10 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
                     case 2: issue_chunk<false, 4>(dcol, abase, bd0, idesc, first); break;
                     case 3: issue_chunk<true, 2>(dcol, abase, bd0, idesc, first); break;
                     case 4: issue_chunk<true, 3>(dcol, abase, bd0, idesc, first); break;
-                    default: issue_chunk<true, 4>(dcol, abase, bd0, idesc, first); break;
+                    case 5: issue_chunk<true, 4>(dcol, abase, bd0, idesc, first); break;
+                    case 6: issue_chunk<false, 2, true>(dcol, abase, bd0, idesc, first); break;
+                    case 7: issue_chunk<false, 3, true>(dcol, abase, bd0, idesc, first); break;
+                    default: issue_chunk<false, 4, true>(dcol, abase, bd0, idesc, first); break;
                 }
                 first = 1u;
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
@@ -1186,7 +1232,7 @@ static int grid_x(int64_t nchunks, int ngroups) {
 
 }  // namespace tc
 
-size_t contract_tc_ws(int64_t nvox, int nshell, int ntri) {
+size_t contract_tc_ws(int64_t nvox, int nshell, int ntri, bool six) {
     // tables (bounded by the largest plan: 8 groups of 512 rows, slots <= ntri
     // + one gap slot per row and shell) + partials + error word
     (void)nshell;
@@ -1195,7 +1241,8 @@ size_t contract_tc_ws(int64_t nvox, int nshell, int ntri) {
                           (size_t)tc::MAXGROUPS * ((size_t)ntri + tc::MAXROWS * tc::MAXB) * 4 + 4096;
     const int64_t nchunks = (nvox + tc::KC - 1) / tc::KC;
     const size_t gx = (size_t)std::min<int64_t>(std::max<int64_t>(nchunks, 1), 1024);
-    return tc::al256(tables) + tc::al256(gx * (size_t)std::max(ntri, 1) * sizeof(double)) + 256;
+    // the 6-product form keeps the partials of both passes
+    return tc::al256(tables) + (six ? 2 : 1) * tc::al256(gx * (size_t)std::max(ntri, 1) * sizeof(double)) + 256;
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -1220,7 +1267,7 @@ static EncodeTiledFn encode_tiled() {
 
 int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_t* tri, const int32_t* tri_host,
                      int ntri, double* bsum, void* ws, size_t ws_bytes, cudaStream_t st, bool run_plan,
-                     bool fine_drain) {
+                     bool fine_drain, bool six) {
     using namespace tc;
     PYSPEC_CHECK_ARG(tri_host != nullptr, "the BF16x3 contraction needs the host copy of the triangle list");
     PYSPEC_CHECK_ARG(nvox % 4 == 0, "BF16x3 contraction needs N^3 divisible by 4");
@@ -1231,7 +1278,7 @@ int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_
         set_error("%s", hp->why);
         return hp->invalid ? PYSPEC_E_INVALID : PYSPEC_E_UNSUPPORTED;
     }
-    const size_t need = contract_tc_ws(nvox, nshell, ntri);
+    const size_t need = contract_tc_ws(nvox, nshell, ntri, six);
     if (ws_bytes < need) {
         set_error("contract workspace %zu bytes < required %zu", ws_bytes, need);
         return PYSPEC_E_WORKSPACE;
@@ -1267,13 +1314,14 @@ int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_
     const int64_t nchunks = (nvox + KC - 1) / KC;
     const int gx = grid_x(nchunks, hp->base.ngroups);
     double* partials = reinterpret_cast<double*>(w + off);
-    if (off + al256((size_t)gx * ntri * sizeof(double)) > ws_bytes) {
+    const int passes = six ? 2 : 1;
+    if (off + al256((size_t)passes * gx * ntri * sizeof(double)) > ws_bytes) {
         set_error("contract workspace too small for %d CTAs", gx);
         return PYSPEC_E_WORKSPACE;
     }
     PYSPEC_CUDA(cudaMemcpyAsync(d_image, hp->image_src, hp->image.size(), cudaMemcpyHostToDevice, st));
     PYSPEC_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), st));
-    PYSPEC_CUDA(cudaMemsetAsync(partials, 0, (size_t)gx * ntri * sizeof(double), st));
+    PYSPEC_CUDA(cudaMemsetAsync(partials, 0, (size_t)passes * gx * ntri * sizeof(double), st));
     Params P = hp->base;
     P.V = nvox;
     P.nchunks = nchunks;
@@ -1283,13 +1331,41 @@ int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_
     P.slot_tri = d_stri;
     P.partials = partials;
     P.err = d_err;
-    P.seg_log2 = fine_drain ? SEG_LOG2_FINE : SEG_LOG2;
+    P.seg_log2 = (fine_drain || six) ? SEG_LOG2_FINE : SEG_LOG2;
+    P.residual = 0;
     PYSPEC_TRY(allow_smem((const void*)contract_tc_kernel, hp->smem));
     contract_tc_kernel<<<dim3(gx, P.ngroups), NTHREADS, hp->smem, st>>>(P, fmap);
     PYSPEC_LAUNCH_CHECK();
     count_launch();
+    if (six) {
+        // The 6-product form.  The first pass sums (P_hi + P_lo)(F_hi + F_lo):
+        // the products and fields to 16 bits.  With x = hi + lo + res (the
+        // third bf16 part, split2_res), the second pass adds
+        // sum_v P_res F_hi + P_hi F_res -- the two largest of the terms the
+        // first pass leaves out (the rest are ~2^-24 of B).  Same rows and
+        // columns; narrow accumulator layout (N columns per tile), two MMAs
+        // per tile and k-step; its own CTA partials, added with the first's.
+        Params R = P;
+        R.residual = 1;
+        R.seg_log2 = SEG_LOG2;       // its terms are ~2^-16 of B: the default drain is ample
+        R.partials = partials + (size_t)gx * ntri;
+        for (int g = 0; g < R.ngroups; ++g) {
+            Group& G = R.g[g];
+            int col = 0;
+            for (int t = 0; t < G.ntiles; ++t) {
+                G.tile_n[t] = (G.tile_n[t] + 15) / 16 * 16;     // narrow: N a multiple of 16
+                G.tile_col[t] = col;
+                col += G.tile_n[t];
+            }
+            G.wide = 0;
+            G.ncols = pow2_cols(col + NSTAGE * MAXTILES * ACOLS);
+        }
+        contract_tc_kernel<<<dim3(gx, R.ngroups), NTHREADS, hp->smem, st>>>(R, fmap);
+        PYSPEC_LAUNCH_CHECK();
+        count_launch();
+    }
     (void)tri;
-    return reduce_partials_launch(partials, gx, ntri, bsum, st);
+    return reduce_partials_launch(partials, passes * gx, ntri, bsum, st);
 }
 
 // Verifies a built plan against its triangle list (see pyspec_bk_plan_check).

@@ -119,7 +119,7 @@ def test_config1_uniform_128_end_to_end():
     half_d = core.fft_periodic_half(xyzs, ws, n, L, float(npart)).clone()
     bsum_d, absum_d, _ = _fp64_sums(half_d, step, jmin, nmax, tri)
     _fresh()
-    for method in ("fp32", "bf16x3", "bf16x3_fine"):
+    for method in ("fp32", "bf16x3", "bf16x3_fine", "bf16x6"):
         got = P.Bk_periodic(xyz, Lbox=L, Ngrid=n, step=step, Ncut=ncut, Nmax=nmax, method=method)
         plan = core.get_plan(n, step, ncut, nmax, method)
         np.testing.assert_array_equal(plan.counts_np, counts)
@@ -152,7 +152,8 @@ def test_config1_uniform_128_end_to_end():
         # clustered 360^3 box (where split-BF16 stays below 1e-5 / 2e-7): here
         # the worst triangles of condition number ~1e3 reach 1.3e-5 with
         # either drain interval (measured 1.30e-5 / 1.24e-5), so the bound is 2e-5
-        bound = {"fp32": (2e-6, 3e-8), "bf16x3": (2e-5, 3e-7), "bf16x3_fine": (2e-5, 1e-7)}[method]
+        bound = {"fp32": (2e-6, 3e-8), "bf16x3": (2e-5, 3e-7), "bf16x3_fine": (2e-5, 1e-7),
+                 "bf16x6": (1e-5, 1e-7)}[method]
         assert con["max_rel_cond_lt_1e3"] <= bound[0]
         assert con["normalised_max"] <= bound[1]
     pk = P.Pk_periodic(xyz, Lbox=L, Ngrid=n)
@@ -176,7 +177,7 @@ def test_config2_all_triangles_fp64():
     assert tri.shape[1] == 6350
     bsum, absum, p0sum = _fp64_sums(half, step, jmin, nmax, tri)
     got = {}
-    for method in ("fp32", "bf16x3", "bf16x3_fine"):
+    for method in ("fp32", "bf16x3", "bf16x3_fine", "bf16x6"):
         plan = core.get_plan(n, step, ncut, nmax, method)
         plan.run(half)
         got[method] = plan.bsum.cpu().numpy()
@@ -196,7 +197,7 @@ def test_config2_all_triangles_fp64():
     _fresh()
     bsum_o, absum_o, _ = _fp64_sums(torch.from_numpy(hz), step, jmin, nmax, tri)
     del hz
-    for method in ("fp32", "bf16x3", "bf16x3_fine"):
+    for method in ("fp32", "bf16x3", "bf16x3_fine", "bf16x6"):
         rep = TF.error_report(got[method], bsum_o, absum_o)
         rep.update(d_rep)
         _report(f"config2_end_to_end_{method}", rep)
@@ -205,6 +206,8 @@ def test_config2_all_triangles_fp64():
     assert c2["config2_contraction_bf16x3"]["normalised_max"] <= 2e-7
     assert c2["config2_contraction_bf16x3_fine"]["max_rel_cond_lt_1e3"] <= 1e-5
     assert c2["config2_contraction_bf16x3_fine"]["normalised_max"] <= 1e-7
+    assert c2["config2_contraction_bf16x6"]["max_rel_cond_lt_1e3"] <= 1e-5
+    assert c2["config2_contraction_bf16x6"]["normalised_max"] <= 1e-7
     assert c2["config2_contraction_fp32"]["max_rel_cond_lt_1e3"] <= 2e-6
     assert c2["config2_contraction_fp32"]["normalised_max"] <= 1e-8
     assert c2["config2_contraction_fp32"]["p0_max_rel"] <= 1e-5

@@ -34,7 +34,7 @@ def _contract(fields, n, tri_slots, method):
     call("pyspec_bk_contract", ptr(fields), n, S, ptr(tri_d), tri_slots.ctypes.data_as(ctypes.c_void_p), T, method,
          ptr(bsum), ptr(ws), ws.numel(), stream_ptr())
     torch.cuda.synchronize()
-    status = int(ws[:4].view(torch.int32).item()) if method == 1 else 0
+    status = int(ws[:4].view(torch.int32).item()) if (method & 0xff) in (1, 2) else 0
     return bsum.cpu().numpy(), status
 
 
@@ -135,3 +135,25 @@ def test_repeated_triangle_rejected(method):
     rc = lib.pyspec_bk_contract(ptr(fields), n, 8, ptr(tri_d), slots.ctypes.data_as(ctypes.c_void_p), T, method,
                                 ptr(bsum), ptr(ws), ws.numel(), stream_ptr())
     assert rc == -1
+
+
+@pytest.mark.parametrize("n,step,nmax", [(48, 1, 40), (40, 1, 60)])
+def test_six_product_form_against_float64(n, step, nmax):
+    """PYSPEC_CONTRACT_BF16X6 (the split-BF16 sums drained every 8 chunks plus
+    a residual pass with the operands' third bf16 parts) on the pair-cover
+    plan (Nmax 40, wide first pass) and a run plan (Nmax 60, narrow first
+    pass): its error, normalised by sum |F_i F_j F_l|, is well below the
+    three-product form's and near the FP32 form's."""
+    jmin = 1
+    fields = _fields(n, step, jmin, nmax, seed=7 * n + nmax)
+    slots = np.ascontiguousarray(core.triangles(jmin, nmax) - jmin, dtype=np.int32)
+    ref, mag = _reference(fields, slots)
+    mag = np.maximum(mag, 1e-300)
+    err = {}
+    for name, method in (("fp32", 0), ("bf16x3", 1), ("bf16x6", 2)):
+        got, status = _contract(fields, n, slots, method)
+        assert status == 0
+        err[name] = np.abs(got - ref) / mag
+    print({k: (float(np.median(v)), float(v.max())) for k, v in err.items()})
+    assert err["bf16x6"].max() < 3e-7
+    assert np.median(err["bf16x6"]) < 0.25 * np.median(err["bf16x3"])
