@@ -115,7 +115,6 @@ struct Params {
     double* partials;            // [gridDim.x][ntri]
     int* err;
     int seg_log2;                // accumulators drained every 2^seg_log2 chunks
-    int residual;                // 1: the residual pass of the 6-product form (see contract_tc_impl)
     int ngroups;
     int maxslots;
     Group g[MAXGROUPS];
@@ -341,8 +340,11 @@ __device__ __forceinline__ float4 lds4(const unsigned char* base, uint32_t off) 
     return *reinterpret_cast<const float4*>(base + off);
 }
 
+template <bool RES>
 __global__ void __launch_bounds__(NTHREADS, 1)
 contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUtensorMap fmap) {
+    // RES: the residual pass of the 6-product form, a separate instantiation
+    // so the 4-product pass keeps its branch-free producer and MMA sequences
     extern __shared__ unsigned char smem_raw[];
     // this CTA's group descriptor, copied out of parameter space once (a
     // runtime index into the parameter struct would otherwise go to the stack)
@@ -520,7 +522,7 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
                 const float4 e = *reinterpret_cast<const float4*>(F + fchunk(ub_r, 2 * ub_g + 1));
                 const float2 x[4] = {make_float2(a.x, a.y), make_float2(a.z, a.w), make_float2(e.x, e.y),
                                      make_float2(e.z, e.w)};
-                if (P.residual) split_store8_res(x, Bst + op_off(brow(ub_r, 0), ub_g), Bst + op_off(brow(ub_r, 1), ub_g));
+                if constexpr (RES) split_store8_res(x, Bst + op_off(brow(ub_r, 0), ub_g), Bst + op_off(brow(ub_r, 1), ub_g));
                 else split_store8(x, Bst + op_off(brow(ub_r, 0), ub_g), Bst + op_off(brow(ub_r, 1), ub_g));
             }
             // A operand: this thread's 8 (or 4) pair rows x 4 voxels of its k-step, straight into TMEM
@@ -532,15 +534,13 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
                 float4 fj[4];
 #pragma unroll
                 for (int y = 0; y < 4; ++y) fj[y] = lds4(F, oj0[y]);
-                if (P.residual) store_slot<true>(fi0, fj, lane_base + acol(s, 2 * tp, kstep));
-                else store_slot(fi0, fj, lane_base + acol(s, 2 * tp, kstep));
+                store_slot<RES>(fi0, fj, lane_base + acol(s, 2 * tp, kstep));
                 if (slot1_on) {
                     if (reload) {
 #pragma unroll
                         for (int y = 0; y < 4; ++y) fj[y] = lds4(F, foff((int)((gs1 >> (8 * y)) & 0xffu)));
                     }
-                    if (P.residual) store_slot<true>(fi1, fj, lane_base + acol(s, 2 * tp + 1, kstep));
-                    else store_slot(fi1, fj, lane_base + acol(s, 2 * tp + 1, kstep));
+                    store_slot<RES>(fi1, fj, lane_base + acol(s, 2 * tp + 1, kstep));
                 }
             }
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
@@ -585,7 +585,7 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
             // apart; the lo blocks are 512 bytes further)
             const uint64_t bdesc0 = make_desc(sbase, 128, wide ? 512 : 1024);
             // tile count 2, 3 or 4 and the form select one branch-free sequence
-            const int mode = (P.residual ? 6 : wide ? 3 : 0) + (ntiles == 2 ? 0 : ntiles == 3 ? 1 : 2);
+            const int mode = (wide ? 3 : 0) + (ntiles == 2 ? 0 : ntiles == 3 ? 1 : 2);
             int seg_count = 0;
             const int seg_mask = (1 << P.seg_log2) - 1;
             uint32_t first = 0;   // 0: the next MMA of each tile overwrites its accumulator
@@ -597,16 +597,21 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
                 // branch between the MMAs of a chunk slows their issue by ~30 %
                 const uint32_t abase = tmem + acol(s, 0, 0);
                 const uint64_t bd0 = bdesc0 + (uint64_t)((s * STAGE_BYTES) >> 4);
-                switch (mode) {
-                    case 0: issue_chunk<false, 2>(dcol, abase, bd0, idesc, first); break;
-                    case 1: issue_chunk<false, 3>(dcol, abase, bd0, idesc, first); break;
-                    case 2: issue_chunk<false, 4>(dcol, abase, bd0, idesc, first); break;
-                    case 3: issue_chunk<true, 2>(dcol, abase, bd0, idesc, first); break;
-                    case 4: issue_chunk<true, 3>(dcol, abase, bd0, idesc, first); break;
-                    case 5: issue_chunk<true, 4>(dcol, abase, bd0, idesc, first); break;
-                    case 6: issue_chunk<false, 2, true>(dcol, abase, bd0, idesc, first); break;
-                    case 7: issue_chunk<false, 3, true>(dcol, abase, bd0, idesc, first); break;
-                    default: issue_chunk<false, 4, true>(dcol, abase, bd0, idesc, first); break;
+                if constexpr (RES) {             // narrow form only (the host sets it)
+                    switch (ntiles) {
+                        case 2: issue_chunk<false, 2, true>(dcol, abase, bd0, idesc, first); break;
+                        case 3: issue_chunk<false, 3, true>(dcol, abase, bd0, idesc, first); break;
+                        default: issue_chunk<false, 4, true>(dcol, abase, bd0, idesc, first); break;
+                    }
+                } else {
+                    switch (mode) {
+                        case 0: issue_chunk<false, 2>(dcol, abase, bd0, idesc, first); break;
+                        case 1: issue_chunk<false, 3>(dcol, abase, bd0, idesc, first); break;
+                        case 2: issue_chunk<false, 4>(dcol, abase, bd0, idesc, first); break;
+                        case 3: issue_chunk<true, 2>(dcol, abase, bd0, idesc, first); break;
+                        case 4: issue_chunk<true, 3>(dcol, abase, bd0, idesc, first); break;
+                        default: issue_chunk<true, 4>(dcol, abase, bd0, idesc, first); break;
+                    }
                 }
                 first = 1u;
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
@@ -1332,9 +1337,8 @@ int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_
     P.partials = partials;
     P.err = d_err;
     P.seg_log2 = (fine_drain || six) ? SEG_LOG2_FINE : SEG_LOG2;
-    P.residual = 0;
-    PYSPEC_TRY(allow_smem((const void*)contract_tc_kernel, hp->smem));
-    contract_tc_kernel<<<dim3(gx, P.ngroups), NTHREADS, hp->smem, st>>>(P, fmap);
+    PYSPEC_TRY(allow_smem((const void*)contract_tc_kernel<false>, hp->smem));
+    contract_tc_kernel<false><<<dim3(gx, P.ngroups), NTHREADS, hp->smem, st>>>(P, fmap);
     PYSPEC_LAUNCH_CHECK();
     count_launch();
     if (six) {
@@ -1346,7 +1350,6 @@ int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_
         // columns; narrow accumulator layout (N columns per tile), two MMAs
         // per tile and k-step; its own CTA partials, added with the first's.
         Params R = P;
-        R.residual = 1;
         R.seg_log2 = SEG_LOG2;       // its terms are ~2^-16 of B: the default drain is ample
         R.partials = partials + (size_t)gx * ntri;
         for (int g = 0; g < R.ngroups; ++g) {
@@ -1360,7 +1363,8 @@ int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_
             G.wide = 0;
             G.ncols = pow2_cols(col + NSTAGE * MAXTILES * ACOLS);
         }
-        contract_tc_kernel<<<dim3(gx, R.ngroups), NTHREADS, hp->smem, st>>>(R, fmap);
+        PYSPEC_TRY(allow_smem((const void*)contract_tc_kernel<true>, hp->smem));
+        contract_tc_kernel<true><<<dim3(gx, R.ngroups), NTHREADS, hp->smem, st>>>(R, fmap);
         PYSPEC_LAUNCH_CHECK();
         count_launch();
     }

@@ -149,11 +149,13 @@ def test_six_product_form_against_float64(n, step, nmax):
     slots = np.ascontiguousarray(core.triangles(jmin, nmax) - jmin, dtype=np.int32)
     ref, mag = _reference(fields, slots)
     mag = np.maximum(mag, 1e-300)
+    live = mag > 1e-300                      # triangles whose shells hold modes on this grid
     err = {}
     for name, method in (("fp32", 0), ("bf16x3", 1), ("bf16x6", 2)):
         got, status = _contract(fields, n, slots, method)
         assert status == 0
-        err[name] = np.abs(got - ref) / mag
+        err[name] = (np.abs(got - ref) / mag)[live]
     print({k: (float(np.median(v)), float(v.max())) for k, v in err.items()})
-    assert err["bf16x6"].max() < 3e-7
+    assert err["bf16x6"].max() < 0.5 * err["bf16x3"].max()
+    assert err["bf16x6"].max() < 5e-7
     assert np.median(err["bf16x6"]) < 0.25 * np.median(err["bf16x3"])
