@@ -6,14 +6,18 @@ Checks that hold at this size:
   (k1 + k2 + k3 = 0 with |k_a| in shells i, j, l; the definition behind
   pyspectrum.py:976-1023) for the low triangles, and integral everywhere;
 * mode counts Nk against the host count;
-* the two contraction forms against each other on every triangle, and both
-  against float64 sums (complex128 shell FFTs of the same delta(k)) on the
-  triangles of shells 1-3."""
+* the contraction forms against float64 sums on every triangle: float64
+  shell fields (complex128 FFTs of the same delta(k)) and float64 triangle
+  sums on the device (oracle/torch_fp64.py, 128 GB for the 60 fields and
+  their absolute values)."""
+import json
+import os
+
 import numpy as np
 import pytest
-import scipy.fft as sfft
 
 from oracle import pyspec_oracle as O
+from oracle import torch_fp64 as TF
 
 pytestmark = pytest.mark.gpu
 
@@ -57,34 +61,40 @@ def test_512_nmax60_counts_contraction_and_fp64():
     half = core.fft_periodic_half(xyzs, ws, N, L, float(x.shape[1]))
     del x, xyzs, ws
     bs = {}
-    for method in ("fp32", "bf16x3"):
+    for method in ("fp32", "bf16x3", "bf16x6"):
         plan = core.get_plan(N, STEP, NCUT, NMAX, method)
         plan.run(half)
         torch.cuda.synchronize()
         bs[method] = plan.bsum.cpu().numpy()
+        if method in core.TENSOR_METHODS:
+            core.check_contract_status(plan.status_word().item())
         assert np.isfinite(bs[method]).all()
-    core.release_plans()
-    torch.cuda.empty_cache()
+        core.release_plans()
+        torch.cuda.empty_cache()
     rel = np.abs(bs["bf16x3"] - bs["fp32"]) / np.abs(bs["fp32"])
     assert np.median(rel) < 1e-4, np.median(rel)
 
-    # float64 reference sums for the triangles of shells 1-3
-    full = O.reflect_delta(half.cpu().numpy().transpose(2, 1, 0), N)
+    # float64 sums of every triangle from the same delta(k)
+    full = TF.reflect_half(half)
     del half
-    kk = np.minimum(np.arange(N), N - np.arange(N)).astype(np.int64)
-    d2 = kk[:, None, None] ** 2 + kk[None, :, None] ** 2 + kk[None, None, :] ** 2
-    irk = O.shell_index_int(d2, STEP)
-    del d2
-    F = {}
-    for j in (1, 2, 3):
-        F[j] = np.real(sfft.fftn(np.where(irk == j, full, 0).astype(np.complex128), workers=-1)).ravel()
-    del full, irk
-    for t in range(loop.shape[1]):
-        i, j, l = (int(v) for v in loop[:, t])
-        if i > 3:
-            continue
-        prod = F[i] * F[j] * F[l]
-        exact, absum = prod.sum(), np.abs(prod).sum()
-        for method in ("fp32", "bf16x3"):
-            err = abs(bs[method][t] - exact) / absum
-            assert err < (2e-6 if method == "fp32" else 2e-5), (method, i, j, l, err)
+    F, _ = TF.shell_fields(full, STEP, jmin, NMAX)
+    del full
+    torch.cuda.empty_cache()
+    exact, absum = TF.triangle_sums(F, loop - jmin)
+    del F
+    torch.cuda.empty_cache()
+    rep = {m: TF.error_report(bs[m], exact, absum) for m in bs}
+    print("config5", json.dumps(rep))
+    out = os.environ.get("PYSPEC_ACCURACY_REPORT")
+    if out:
+        try:
+            with open(out) as f:
+                prev = json.load(f)
+        except (OSError, ValueError):
+            prev = {}
+        prev.update({f"config5_{m}": v for m, v in rep.items()})
+        with open(out, "w") as f:
+            json.dump(prev, f, indent=1)
+    assert rep["fp32"]["normalised_max"] < 5e-8
+    assert rep["bf16x3"]["normalised_max"] < 5e-7
+    assert rep["bf16x6"]["normalised_max"] < 2e-7
