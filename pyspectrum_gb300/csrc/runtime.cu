@@ -1,5 +1,8 @@
 // Error reporting, launch accounting and FFT radix planning.
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <utility>
 #include <stdarg.h>
 #include <string.h>
 #include "common.cuh"
@@ -54,13 +57,24 @@ extern "C" int pyspec_last_error(char* buf, size_t len) {
 extern "C" int64_t pyspec_launch_count(void) { return pyspec::g_launches.load(); }
 
 namespace pyspec {
+// The opt-in limit covers static + dynamic shared memory: a launch whose
+// dynamic bytes alone stay under the 48 KB default can still exceed it, so
+// the attribute is raised for any size above what this function (on this
+// device) was last given.
 int allow_smem(const void* func, size_t bytes) {
-    if (bytes <= 48 * 1024) return PYSPEC_OK;
     if (bytes > 227 * 1024) {
         set_error("kernel needs %zu bytes of shared memory (limit 227 KB)", bytes);
         return PYSPEC_E_UNSUPPORTED;
     }
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, size_t> raised;
+    int dev = 0;
+    PYSPEC_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& cur = raised[{func, dev}];
+    if (bytes <= cur) return PYSPEC_OK;
     PYSPEC_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    cur = bytes;
     return PYSPEC_OK;
 }
 
