@@ -62,6 +62,11 @@ extern "C" {
  * of every 32.  The split-BF16 error is set by the length of that FP32
  * accumulation, so this trades drain time for about 4x smaller errors. */
 #define PYSPEC_CONTRACT_FINE_DRAIN 0x200
+/* Flag OR-ed into a tensor-core method: keep 32-voxel chunks.  By default a
+ * plan of 2 or 3 tiles in the wide MMA form whose buffers fit in shared
+ * memory runs with 64-voxel chunks (one hand-over per 64 voxels; the A_lo
+ * operand in shared memory); same sums, for the autotuner, which times both. */
+#define PYSPEC_CONTRACT_KC32 0x400
 
 int pyspec_abi_version(void);
 
@@ -219,12 +224,14 @@ int pyspec_bk_contract(const float *fields, int ngrid, int nshell, const int32_t
  * two largest shells), [3] MMAs per 32 voxels summed over groups, [4] Kahan
  * slots of group 0, [5] 1 if group 0 uses the wide MMA form, [6] tensor-core
  * multiply-adds per voxel summed over groups (the executed work), [7] shared-
- * memory bank clashes between the producer threads that share load phases.
+ * memory bank clashes between the producer threads that share load phases,
+ * [8] voxels per chunk (64 or 32) the contraction runs with.
  * Returns 0; PYSPEC_E_INVALID / PYSPEC_E_UNSUPPORTED where the contraction
  * would; PYSPEC_E_INVALID with a message if the plan fails the check.
  * ---------------------------------------------------------------------- */
 int pyspec_bk_plan_check(int nshell, const int32_t *tri_host, int ntri, int64_t *info, int ninfo);
-/* The same for the plan that method flags `flags` (0 or PYSPEC_CONTRACT_RUN_PLAN) select. */
+/* The same for the plan that method flags `flags` (PYSPEC_CONTRACT_RUN_PLAN,
+ * PYSPEC_CONTRACT_KC32 or both) select. */
 int pyspec_bk_plan_check_flags(int nshell, const int32_t *tri_host, int ntri, int flags, int64_t *info,
                                int ninfo);
 

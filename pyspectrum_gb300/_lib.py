@@ -61,6 +61,7 @@ CONTRACT_BF16X3 = 1
 CONTRACT_BF16X6 = 2
 CONTRACT_RUN_PLAN = 0x100
 CONTRACT_FINE_DRAIN = 0x200
+CONTRACT_KC32 = 0x400
 
 
 class PyspecError(RuntimeError):

@@ -641,7 +641,7 @@ extern "C" int pyspec_bk_normalize(const double* bsum, const int64_t* counts, co
 }
 
 extern "C" size_t pyspec_bk_contract_workspace(int ngrid, int nshell, int ntri, int method) {
-    method &= ~(PYSPEC_CONTRACT_RUN_PLAN | PYSPEC_CONTRACT_FINE_DRAIN);
+    method &= ~(PYSPEC_CONTRACT_RUN_PLAN | PYSPEC_CONTRACT_FINE_DRAIN | PYSPEC_CONTRACT_KC32);
     if (ngrid < 2 || nshell < 1 || ntri < 0) return 0;
     const int64_t V = (int64_t)ngrid * ngrid * ngrid;
     if (method == PYSPEC_CONTRACT_BF16X3) return contract_tc_ws(V, nshell, ntri);
@@ -664,10 +664,11 @@ extern "C" int pyspec_bk_contract(const float* fields, int ngrid, int nshell, co
     cudaStream_t st = as_stream(stream);
     const bool run_plan = (method & PYSPEC_CONTRACT_RUN_PLAN) != 0;
     const bool fine_drain = (method & PYSPEC_CONTRACT_FINE_DRAIN) != 0;
-    method &= ~(PYSPEC_CONTRACT_RUN_PLAN | PYSPEC_CONTRACT_FINE_DRAIN);
-    PYSPEC_CHECK_ARG((!run_plan && !fine_drain) || method == PYSPEC_CONTRACT_BF16X3 ||
+    const bool kc32 = (method & PYSPEC_CONTRACT_KC32) != 0;
+    method &= ~(PYSPEC_CONTRACT_RUN_PLAN | PYSPEC_CONTRACT_FINE_DRAIN | PYSPEC_CONTRACT_KC32);
+    PYSPEC_CHECK_ARG((!run_plan && !fine_drain && !kc32) || method == PYSPEC_CONTRACT_BF16X3 ||
                          method == PYSPEC_CONTRACT_BF16X6,
-                     "PYSPEC_CONTRACT_RUN_PLAN and PYSPEC_CONTRACT_FINE_DRAIN apply to the tensor-core methods only");
+                     "PYSPEC_CONTRACT_RUN_PLAN, _FINE_DRAIN and _KC32 apply to the tensor-core methods only");
     if (method == PYSPEC_CONTRACT_FP32) {
         if (tri_host == nullptr)   // device-only triangle list: the unplanned kernel
             return contract_simple_impl<float>(fields, V, nshell, tri, ntri, nullptr, V, bsum,
@@ -676,10 +677,10 @@ extern "C" int pyspec_bk_contract(const float* fields, int ngrid, int nshell, co
     }
     if (method == PYSPEC_CONTRACT_BF16X3)
         return contract_tc_impl(fields, V, nshell, tri, tri_host, ntri, bsum, workspace, ws_bytes, st, run_plan,
-                                fine_drain);
+                                fine_drain, false, kc32);
     if (method == PYSPEC_CONTRACT_BF16X6)
         return contract_tc_impl(fields, V, nshell, tri, tri_host, ntri, bsum, workspace, ws_bytes, st, run_plan,
-                                true, true);
+                                true, true, kc32);
     set_error("unknown contraction method %d", method);
     return PYSPEC_E_INVALID;
 }

@@ -22,7 +22,7 @@ int contract_fp32_need(int64_t nvox, int nshell, const int32_t* tri_host, int nt
 size_t contract_tc_ws(int64_t nvox, int nshell, int ntri, bool six = false);
 int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_t* tri, const int32_t* tri_host,
                      int ntri, double* bsum, void* ws, size_t ws_bytes, cudaStream_t st, bool run_plan = false,
-                     bool fine_drain = false, bool six = false);
+                     bool fine_drain = false, bool six = false, bool kc32 = false);
 
 // bsum[t] = sum over nblk rows of partials[b][t] (float64, fixed order)
 int reduce_partials_launch(const double* partials, int nblk, int ntri, double* bsum, cudaStream_t st);

@@ -675,6 +675,373 @@ contract_tc_kernel(const __grid_constant__ Params P, const __grid_constant__ CUt
 }
 
 // ---------------------------------------------------------------------------
+// Deep-chunk form: 64 voxels (four k-steps) per hand-over, for plans of 2 or
+// 3 tiles that are all wide.  Each producer warp, the MMA thread and the
+// copy thread pay their per-chunk synchronisation (waits, fences, arrivals,
+// commit) once per 64 voxels instead of once per 32 -- that fixed cost, not
+// the work, bounds the 32-voxel kernel.  TMEM keeps the same layout (A_hi of
+// a tile and stage: 4 k-steps x 8 columns = 32), the A_lo parts go to shared
+// memory (16 KB per tile and stage, K-major core matrices, 64 k per 8-row
+// block) and the MMAs read them through descriptors.  Per tile and k-step:
+// A_hi (TMEM) and A_lo (shared memory) against all 2N interleaved B rows.
+// ---------------------------------------------------------------------------
+constexpr int KC64 = 64;
+constexpr int STAGE64_BYTES = BROWS * KC64 * 2;     // B operand of one stage: 16 KB
+constexpr int ALO_TILE_BYTES = 128 * KC64 * 2;      // A_lo of one tile and stage: 16 KB
+constexpr int SEG64_SHIFT = 1;                       // drains every 2^(seg_log2 - 1) deep chunks (same voxels)
+constexpr int kDeepSmemLimit = 232448 - 6144;        // dynamic bytes: the 227 KB opt-in less the static arrays
+
+// dynamic shared memory before the Kahan slots, for nfbuf field buffers of two halves
+__host__ __device__ constexpr int fixed_smem64(int nshell, int ntiles, int nfbuf) {
+    return 1024 + nfbuf * 2 * f_bytes(nshell) + NSTAGE * STAGE64_BYTES + NSTAGE * ntiles * ALO_TILE_BYTES;
+}
+
+// K-major no-swizzle operand with 64 k per row block: core matrix (r/8, g) at
+// (r/8)*1024 + g*128, row r%8 at 16 B
+__device__ __forceinline__ int op_off64(int r, int kgroup) { return (r >> 3) * 1024 + kgroup * 128 + (r & 7) * 16; }
+
+// tcgen05.st 16x256b.x1: repeat 0 of the x2 shape (8 columns)
+__device__ __forceinline__ void tmem_st16x256_x1(uint32_t addr, const uint32_t* v) {
+    asm volatile("tcgen05.st.sync.aligned.16x256b.x1.b32 [%0], {%1,%2,%3,%4};"
+                 :: "r"(addr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]) : "memory");
+}
+
+// One slot of a producer thread for one k-step: the hi parts of its four
+// rows into TMEM (lanes x + 8y of the quarter, 8 columns at `addr`), the lo
+// parts into the tile's A_lo block (`alo` = this thread's address for row
+// y = 0; row y lies in the next 8-row block, y * 1024 bytes further).
+__device__ __forceinline__ void store_slot64(float4 fi, const float4* fj, uint32_t addr, char* alo) {
+#pragma unroll
+    for (int blk = 0; blk < 2; ++blk) {
+        uint32_t h[4], l[4];
+#pragma unroll
+        for (int yy = 0; yy < 2; ++yy) {
+            const float4 f = fj[2 * blk + yy];
+            const float2 p0 = mul2(make_float2(fi.x, fi.y), make_float2(f.x, f.y));
+            const float2 p1 = mul2(make_float2(fi.z, fi.w), make_float2(f.z, f.w));
+            split2(p0, h[2 * yy], l[2 * yy]);
+            split2(p1, h[2 * yy + 1], l[2 * yy + 1]);
+        }
+        tmem_st16x256_x1(addr + ((uint32_t)(16 * blk) << 16), h);
+        // rows y = 2 blk and 2 blk + 1 sit in 8-row blocks 2 blk and 2 blk + 1 of the quarter
+        *reinterpret_cast<uint2*>(alo + (2 * blk) * 1024) = make_uint2(l[0], l[1]);
+        *reinterpret_cast<uint2*>(alo + (2 * blk + 1) * 1024) = make_uint2(l[2], l[3]);
+    }
+}
+
+// The MMAs of one deep chunk (all tiles wide): per k-step and tile, A_hi from
+// TMEM (`abase` + 32 t + 8 ks) and A_lo from shared memory (`alo0` + 16 KB t
+// + 256 ks) against the stage's B rows (`bd0` + 256 ks, 8-row blocks 1024
+// bytes apart).
+template <int NT>
+__device__ __forceinline__ void issue_chunk64(const uint32_t (&dcol)[MAXTILES], uint32_t abase, uint64_t alo0,
+                                              uint64_t bd0, const uint32_t (&idesc)[MAXTILES], uint32_t first) {
+#pragma unroll
+    for (int ks = 0; ks < KC64 / 16; ++ks) {
+        const uint32_t acc0 = ks == 0 ? first : 1u;
+        const uint64_t bd = bd0 + (uint64_t)((ks * 256) >> 4);
+#pragma unroll
+        for (int t = 0; t < NT; ++t) {
+            const uint32_t ahi = abase + (uint32_t)(t * ACOLS + ks * 8);
+            const uint64_t alo = alo0 + (uint64_t)((t * ALO_TILE_BYTES + ks * 256) >> 4);
+            asm volatile("{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n"
+                         :: "r"(dcol[t]), "r"(ahi), "l"(bd), "r"(idesc[t]), "r"(acc0));
+            asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, 1;"
+                         :: "r"(dcol[t]), "l"(alo), "l"(bd), "r"(idesc[t]));
+        }
+    }
+}
+
+template <int NFB>
+__global__ void __launch_bounds__(NTHREADS, 1)
+contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ CUtensorMap fmap) {
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ Group G;
+    __shared__ __align__(8) uint64_t bar_full[NSTAGE], bar_empty[NSTAGE], bar_ffull[NFB], bar_fempty[NFB];
+    __shared__ __align__(8) uint64_t bar_seg, bar_drained;
+    __shared__ uint32_t tmem_slot;
+    __shared__ __align__(8) int16_t pij[MAXROWS * 4];
+    __shared__ int abort_flag_s;
+    volatile int& abort_flag = abort_flag_s;
+    if (threadIdx.x == 0) G = P.g[blockIdx.y];
+    const uint32_t raw_u32 = smem_u32(smem_raw);
+    unsigned char* smem = smem_raw + (((raw_u32 + 1023u) & ~1023u) - raw_u32);
+    const int F_BYTES = f_bytes(P.nshell);                                   // one 32-voxel half
+    unsigned char* fbuf = smem;                                              // NFB x 2 halves
+    unsigned char* stage_base = smem + NFB * 2 * F_BYTES;                    // NSTAGE x B operand
+    __syncthreads();
+    const int ntl = G.ntiles;
+    unsigned char* alo_base = stage_base + NSTAGE * STAGE64_BYTES;            // NSTAGE x ntiles x A_lo
+    float2* acc = reinterpret_cast<float2*>(alo_base + NSTAGE * ntl * ALO_TILE_BYTES);
+
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int64_t c0 = (int64_t)blockIdx.x * P.chunks_per_cta;
+    const int64_t c1 = min(P.nchunks, c0 + P.chunks_per_cta);
+    const int nch = (int)max((int64_t)0, c1 - c0);
+    int C = 0;
+    for (int t = 0; t < ntl; ++t) C = max(C, G.tile_col[t] + 2 * G.tile_n[t]);
+
+    for (int i = tid; i < MAXROWS * 4; i += NTHREADS) pij[i] = P.pair_row[(size_t)G.table_off * 4 + i];
+    for (int i = tid; i < G.nslots; i += NTHREADS) acc[i] = make_float2(0.f, 0.f);
+    for (int i = tid; i < NSTAGE * STAGE64_BYTES / 16; i += NTHREADS)
+        reinterpret_cast<uint4*>(stage_base)[i] = make_uint4(0, 0, 0, 0);
+    if (tid == 0) {
+        abort_flag = 0;
+        for (int s = 0; s < NSTAGE; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_full[s])), "r"(PWARPS));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_empty[s])), "r"(1));
+        }
+        for (int b = 0; b < NFB; ++b) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_ffull[b])), "r"(1));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_fempty[b])), "r"(PWARPS));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_seg)), "r"(1));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_drained)), "r"(PWARPS));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == MMA_WARP) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_u32(&tmem_slot)), "r"(G.ncols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    const int q = warp & 3;
+    const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+    // A_hi of tile t, stage s, k-step ks (0..3): 8 columns
+    auto acol = [&](int s, int t, int ks) { return (uint32_t)(C + (s * MAXTILES + t) * ACOLS + ks * 8); };
+    const int seg_log2 = P.seg_log2 - SEG64_SHIFT;
+
+    if (warp < PWARPS) {
+        // ================= producers =================
+        // As in the 32-voxel kernel, warp w owns TMEM lane quarter w % 4 of
+        // tile pair (w / 4) % 2; it forms k-steps (w / 8) % 2 and (w / 8) % 2
+        // + 2 of each chunk (the same 16-voxel position in both 32-voxel halves).
+        const int rows = G.rows;
+        const int nsh = P.nshell;
+        const int tp = (warp >> 2) & 1;
+        const int kstep = (warp >> 3) & 1;
+        const uint32_t kx = kstep ? 64u : 0u;
+        const bool tp_on = 2 * tp < ntl;
+        const bool slot1_on = 2 * tp + 1 < ntl;
+        const int ax = lane & 3;
+        const int xr = lane >> 2;
+        const int32_t* rtw = P.rt_tab + ((size_t)blockIdx.y * RT_PER_GROUP + tp * 32 + q * 8 + xr) * RT_WORDS;
+        const uint32_t code = (uint32_t)rtw[0];
+        const uint32_t gs0 = (uint32_t)rtw[1], gs1 = (uint32_t)rtw[2];
+        auto foff = [&](int r) {
+            r = min(r, nsh - 1);
+            return (uint32_t)(r * 128 + ((ax ^ (r & 7)) << 4)) ^ kx;
+        };
+        const uint32_t oi0 = foff((int)(code & 0xffu)), oi1 = foff((int)((code >> 8) & 0xffu));
+        const bool reload = gs1 != gs0;
+        uint32_t oj0[4];
+#pragma unroll
+        for (int y = 0; y < 4; ++y) oj0[y] = foff((int)((gs0 >> (8 * y)) & 0xffu));
+        // this thread's A_lo byte offset inside a tile block for k-step
+        // kstep (k-step kstep + 2 of the second half: k-groups 4 further,
+        // + 512 bytes): row 32q + xr (y = 0), k-group 2 kstep + ax / 2,
+        // bytes (ax % 2) * 8
+        const int alo_thr = (4 * q) * 1024 + (2 * kstep + (ax >> 1)) * 128 + xr * 16 + (ax & 1) * 8;
+        // B writer: shell r, k-group g (voxels 8g..8g+7 of the 64); 8 nshell <= 512 threads
+        int ub_r = -1, ub_g = 0;
+        const bool b_warp = (warp * 32) < nsh * 8;
+        if (tid < nsh * 8) {
+            ub_g = tid / nsh;
+            ub_r = tid - ub_g * nsh;
+        }
+        const int seg_len = 1 << seg_log2;
+        const int nseg = (nch + seg_len - 1) >> seg_log2;
+        int seg_count = 0;
+        bool failed = false;
+        auto drain = [&]() -> bool {
+            if (!warp_wait(smem_u32(&bar_seg), seg_count & 1)) return false;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            for (int cg = 16 * ((warp >> 2) & 3); cg < C; cg += 64) {
+                uint32_t d[16];
+                tmem_ld8(lane_base + (uint32_t)cg, d);
+                tmem_ld8(lane_base + (uint32_t)cg + 8u, d + 8);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                int t = 0;
+                while (t + 1 < ntl && cg >= G.tile_col[t + 1]) ++t;
+                const int drow = 128 * t + 32 * q + lane;
+                const short4 pr = drow < rows ? *reinterpret_cast<const short4*>(&pij[4 * drow])
+                                              : make_short4(-1, 0, -1, 0);
+                const int sh0 = (cg - G.tile_col[t]) >> 1;
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int l = sh0 + e;
+                    if (pr.x < 0 || l < pr.y || l > pr.z) continue;
+                    const int slot = pr.w + (l - pr.y);
+                    const float v = __uint_as_float(d[e]) + __uint_as_float(d[e + 8]);
+                    const float2 a = acc[slot];
+                    const float y = v - a.y;
+                    const float sum = a.x + y;
+                    acc[slot] = make_float2(sum, (sum - a.x) - y);
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&bar_drained));
+            ++seg_count;
+            return true;
+        };
+        for (int c = 0; c < nch; ++c) {
+            if (__any_sync(0xffffffffu, abort_flag != 0)) { failed = true; break; }
+            const int s = c & 1;
+            const int b = c % NFB;
+            if (!warp_wait(smem_u32(&bar_ffull[b]), (uint32_t)(c / NFB) & 1u)) {
+                atomicExch(P.err, 1);
+                abort_flag = 1;
+                failed = true;
+                break;
+            }
+            if (c >= NSTAGE) {
+                if (!warp_wait(smem_u32(&bar_empty[s]), ((c - NSTAGE) >> 1) & 1)) {
+                    atomicExch(P.err, 1);
+                    abort_flag = 1;
+                    failed = true;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            }
+            const unsigned char* F = fbuf + (size_t)b * 2 * F_BYTES;
+            char* Bst = reinterpret_cast<char*>(stage_base) + (size_t)s * STAGE64_BYTES;
+            char* Alo = reinterpret_cast<char*>(alo_base) + (size_t)s * ntl * ALO_TILE_BYTES;
+            if (ub_r >= 0) {
+                const unsigned char* Fh = F + (ub_g >> 2) * F_BYTES;
+                const int g4 = ub_g & 3;
+                const float4 a = *reinterpret_cast<const float4*>(Fh + fchunk(ub_r, 2 * g4));
+                const float4 e = *reinterpret_cast<const float4*>(Fh + fchunk(ub_r, 2 * g4 + 1));
+                const float2 x[4] = {make_float2(a.x, a.y), make_float2(a.z, a.w), make_float2(e.x, e.y),
+                                     make_float2(e.z, e.w)};
+                split_store8(x, Bst + op_off64(brow(ub_r, 0), ub_g), Bst + op_off64(brow(ub_r, 1), ub_g));
+            }
+            if (tp_on) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const unsigned char* Fh = F + h * F_BYTES;
+                    const int ks = kstep + 2 * h;
+                    const float4 fi0 = lds4(Fh, oi0);
+                    const float4 fi1 = slot1_on ? lds4(Fh, oi1) : fi0;
+                    float4 fj[4];
+#pragma unroll
+                    for (int y = 0; y < 4; ++y) fj[y] = lds4(Fh, oj0[y]);
+                    store_slot64(fi0, fj, lane_base + acol(s, 2 * tp, ks),
+                                 Alo + (2 * tp) * ALO_TILE_BYTES + alo_thr + h * 512);
+                    if (slot1_on) {
+                        if (reload) {
+#pragma unroll
+                            for (int y = 0; y < 4; ++y) fj[y] = lds4(Fh, foff((int)((gs1 >> (8 * y)) & 0xffu)));
+                        }
+                        store_slot64(fi1, fj, lane_base + acol(s, 2 * tp + 1, ks),
+                                     Alo + (2 * tp + 1) * ALO_TILE_BYTES + alo_thr + h * 512);
+                    }
+                }
+            }
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+            // A_lo and B writes (generic proxy) made visible to the MMA (async proxy)
+            if (tp_on || b_warp) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(smem_u32(&bar_full[s]));
+                mbar_arrive(smem_u32(&bar_fempty[b]));
+            }
+            while (seg_count < nseg && ((seg_count + 1) << seg_log2) - 1 < c) {
+                if (!drain()) { atomicExch(P.err, 2); abort_flag = 1; failed = true; break; }
+            }
+            if (failed) break;
+        }
+        while (!failed && seg_count < nseg) {
+            if (!drain()) { atomicExch(P.err, 2); abort_flag = 1; break; }
+        }
+    } else if (warp == MMA_WARP) {
+        if (lane == 0) {
+            uint32_t idesc[MAXTILES], dcol[MAXTILES];
+#pragma unroll
+            for (int t = 0; t < MAXTILES; ++t) {
+                idesc[t] = make_idesc(128, 2 * G.tile_n[t]);
+                dcol[t] = tmem + (uint32_t)G.tile_col[t];
+            }
+            const uint64_t bdesc0 = make_desc(smem_u32(stage_base), 128, 1024);
+            const uint64_t adesc0 = make_desc(smem_u32(alo_base), 128, 1024);
+            int seg_count = 0;
+            const int seg_mask = (1 << seg_log2) - 1;
+            uint32_t first = 0;
+            for (int c = 0; c < nch; ++c) {
+                const int s = c & 1;
+                if (!mbar_wait(smem_u32(&bar_full[s]), (c >> 1) & 1)) { atomicExch(P.err, 3); abort_flag = 1; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t abase = tmem + acol(s, 0, 0);
+                const uint64_t bd0 = bdesc0 + (uint64_t)((s * STAGE64_BYTES) >> 4);
+                const uint64_t alo0 = adesc0 + (uint64_t)((s * ntl * ALO_TILE_BYTES) >> 4);
+                if (ntl == 2) issue_chunk64<2>(dcol, abase, alo0, bd0, idesc, first);
+                else issue_chunk64<3>(dcol, abase, alo0, bd0, idesc, first);
+                first = 1u;
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                             :: "r"(smem_u32(&bar_empty[s])) : "memory");
+                if (((c + 1) & seg_mask) == 0 || c + 1 == nch) {
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                                 :: "r"(smem_u32(&bar_seg)) : "memory");
+                    if (!mbar_wait(smem_u32(&bar_drained), seg_count & 1)) { atomicExch(P.err, 4); abort_flag = 1; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    ++seg_count;
+                    first = 0u;
+                }
+            }
+            if (nch > 0) {
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                             :: "r"(smem_u32(&bar_seg)) : "memory");
+                mbar_wait(smem_u32(&bar_seg), seg_count & 1);
+            }
+        }
+    } else if (warp == TMA_WARP && lane == 0) {
+        // two 32-voxel copies per chunk into the buffer's halves, one barrier
+        const uint32_t fb0 = smem_u32(fbuf);
+        const uint32_t tx = (uint32_t)(P.nshell * KC64 * 4);
+        int issued = 0;
+        for (int c = 0; c < nch; ++c) {
+            const int b = c % NFB;
+            if (c >= NFB && !mbar_wait(smem_u32(&bar_fempty[b]), (uint32_t)(c / NFB - 1) & 1u)) {
+                atomicExch(P.err, 5);
+                abort_flag = 1;
+                break;
+            }
+            if (abort_flag) break;
+            const uint32_t fb = smem_u32(&bar_ffull[b]);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(fb), "r"(tx) : "memory");
+            const int x0 = (int)((c0 + c) * KC64);
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                asm volatile(
+                    "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+                    :: "r"(fb0 + (uint32_t)((2 * b + h) * F_BYTES)), "l"(reinterpret_cast<uint64_t>(&fmap)),
+                       "r"(x0 + 32 * h), "r"(0), "r"(fb)
+                    : "memory");
+            issued = c + 1;
+        }
+        for (int c = max(0, issued - NFB); c < issued; ++c)
+            mbar_wait(smem_u32(&bar_ffull[c % NFB]), (uint32_t)(c / NFB) & 1u);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (!abort_flag) {
+        for (int i = tid; i < G.nslots; i += NTHREADS) {
+            const int t = P.slot_tri[(size_t)blockIdx.y * P.maxslots + i];
+            if (t >= 0) P.partials[(size_t)blockIdx.x * P.ntri + t] = (double)acc[i].x - (double)acc[i].y;
+        }
+    }
+    if (warp == MMA_WARP) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(G.ncols));
+    }
+}
+
+// ---------------------------------------------------------------------------
 // host planning, two kinds of plan (cached per triangle list):
 //  - runs: pairs (i, j) = the two largest shell slots of each triangle,
 //    column = the smallest.  The pairs of each shell i are cut into runs of
@@ -700,6 +1067,8 @@ struct HostPlan {
     bool ok = false;
     bool invalid = false;         // the triangle list itself is malformed (vs. unsupported)
     bool cover = false;           // rows are a pair cover (3 tiles), not runs
+    int nfb64 = 0;                // field buffers of the 64-voxel kernel (0: the plan does not fit it)
+    size_t smem64 = 0;            // its dynamic shared memory
     char why[160] = {0};
 };
 
@@ -751,6 +1120,24 @@ static void finish_plan(HostPlan* hp, int ngroups, int maxslots, const std::vect
     hp->image_src = pinned_copy(hp->image.data(), hp->image.size());
     if (hp->image_src == nullptr) hp->image_src = hp->image.data();
     hp->ok = true;
+    // the 64-voxel kernel: every group of 2 or 3 tiles in the wide form, and
+    // its buffers (two or three field buffers) in shared memory
+    bool deep = true;
+    int ntmax = 0;
+    for (int g = 0; g < ngroups; ++g) {
+        const Group& G = P.g[g];
+        deep = deep && (G.ntiles == 2 || G.ntiles == 3) && G.wide;
+        ntmax = std::max(ntmax, G.ntiles);
+    }
+    const int nshell = P.nshell;
+    for (int nfb = 3; deep && nfb >= 2; --nfb) {
+        const size_t need = (size_t)fixed_smem64(nshell, ntmax, nfb) + sizeof(float2) * (size_t)maxslots;
+        if (need <= (size_t)kDeepSmemLimit) {
+            hp->nfb64 = nfb;
+            hp->smem64 = need;
+            break;
+        }
+    }
 }
 
 // Cover plan: a D row (a, b) gives B(a, b, c) for every column c, so the rows
@@ -1272,7 +1659,7 @@ static EncodeTiledFn encode_tiled() {
 
 int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_t* tri, const int32_t* tri_host,
                      int ntri, double* bsum, void* ws, size_t ws_bytes, cudaStream_t st, bool run_plan,
-                     bool fine_drain, bool six) {
+                     bool fine_drain, bool six, bool kc32) {
     using namespace tc;
     PYSPEC_CHECK_ARG(tri_host != nullptr, "the BF16x3 contraction needs the host copy of the triangle list");
     PYSPEC_CHECK_ARG(nvox % 4 == 0, "BF16x3 contraction needs N^3 divisible by 4");
@@ -1337,8 +1724,21 @@ int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_
     P.partials = partials;
     P.err = d_err;
     P.seg_log2 = (fine_drain || six) ? SEG_LOG2_FINE : SEG_LOG2;
-    PYSPEC_TRY(allow_smem((const void*)contract_tc_kernel<false>, hp->smem));
-    contract_tc_kernel<false><<<dim3(gx, P.ngroups), NTHREADS, hp->smem, st>>>(P, fmap);
+    if (hp->nfb64 > 0 && !kc32) {
+        // 64-voxel chunks: the same CTAs, half the chunks
+        Params D = P;
+        D.nchunks = (nvox + KC64 - 1) / KC64;
+        D.chunks_per_cta = (D.nchunks + gx - 1) / gx;
+        const void* fn = hp->nfb64 == 3 ? (const void*)contract_tc64_kernel<3> : (const void*)contract_tc64_kernel<2>;
+        PYSPEC_TRY(allow_smem(fn, hp->smem64));
+        if (hp->nfb64 == 3)
+            contract_tc64_kernel<3><<<dim3(gx, D.ngroups), NTHREADS, hp->smem64, st>>>(D, fmap);
+        else
+            contract_tc64_kernel<2><<<dim3(gx, D.ngroups), NTHREADS, hp->smem64, st>>>(D, fmap);
+    } else {
+        PYSPEC_TRY(allow_smem((const void*)contract_tc_kernel<false>, hp->smem));
+        contract_tc_kernel<false><<<dim3(gx, P.ngroups), NTHREADS, hp->smem, st>>>(P, fmap);
+    }
     PYSPEC_LAUNCH_CHECK();
     count_launch();
     if (six) {
@@ -1431,7 +1831,7 @@ extern "C" int pyspec_bk_plan_check_flags(int nshell, const int32_t* tri_host, i
     using namespace pyspec::tc;
     PYSPEC_CHECK_ARG(tri_host != nullptr && ntri > 0, "empty or NULL triangle list");
     PYSPEC_CHECK_ARG(nshell >= 1 && ninfo >= 0 && (info != nullptr || ninfo == 0), "bad arguments");
-    PYSPEC_CHECK_ARG((flags & ~PYSPEC_CONTRACT_RUN_PLAN) == 0, "unknown plan flags 0x%x", flags);
+    PYSPEC_CHECK_ARG((flags & ~(PYSPEC_CONTRACT_RUN_PLAN | PYSPEC_CONTRACT_KC32)) == 0, "unknown plan flags 0x%x", flags);
     HostPlan* hp = get_plan(nshell, tri_host, ntri, (flags & PYSPEC_CONTRACT_RUN_PLAN) != 0);
     if (!hp->ok) {
         set_error("%s", hp->why);
@@ -1464,8 +1864,8 @@ extern "C" int pyspec_bk_plan_check_flags(int nshell, const int32_t* tri_host, i
             if (a[2] != a[1] || b[2] != b[1])
                 for (int y = 0; y < 4; ++y) clashes += clash((a[2] >> (8 * y)) & 0xff, (b[2] >> (8 * y)) & 0xff);
         }
-    const int64_t vals[8] = {P.ngroups, P.g[0].ntiles, hp->cover ? 1 : 0, mma, P.g[0].nslots, P.g[0].wide, macs,
-                             clashes};
-    for (int k = 0; k < ninfo && k < 8; ++k) info[k] = vals[k];
+    const int64_t vals[9] = {P.ngroups, P.g[0].ntiles, hp->cover ? 1 : 0, mma, P.g[0].nslots, P.g[0].wide, macs,
+                             clashes, (hp->nfb64 > 0 && !(flags & PYSPEC_CONTRACT_KC32)) ? KC64 : KC};
+    for (int k = 0; k < ninfo && k < 9; ++k) info[k] = vals[k];
     return PYSPEC_OK;
 }

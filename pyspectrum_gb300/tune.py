@@ -225,14 +225,16 @@ def fft3d(grid, n, sign=1):
 # ---------------------------------------------------------------------------
 def contract_flags(plan) -> int:
     """Method flags of the tuned tile plan for a BkPlan's triangle list
-    (0: the default, pair cover where it needs fewer tiles; or
-    CONTRACT_RUN_PLAN), timed on the plan's current fields the first time."""
+    (0: the default, pair cover where it needs fewer tiles and 64-voxel
+    chunks where the plan allows them; CONTRACT_KC32: 32-voxel chunks;
+    CONTRACT_RUN_PLAN, with either), timed on the plan's current fields the
+    first time."""
     from .core import METHODS, TENSOR_METHODS
     if plan.method not in TENSOR_METHODS or not enabled():
         return 0
     digest = hashlib.sha1(plan.slots_host.tobytes()).hexdigest()[:16]
     key = f"contract|{_device_key(plan.device)}|{plan.method}|n{plan.n}|S{plan.S}|T{plan.T}|{digest}"
-    cands = [0, _lib.CONTRACT_RUN_PLAN]
+    cands = [0, _lib.CONTRACT_KC32, _lib.CONTRACT_RUN_PLAN, _lib.CONTRACT_RUN_PLAN | _lib.CONTRACT_KC32]
 
     def run(flags):
         call("pyspec_bk_contract", ptr(plan.fields), plan.n, plan.S, ptr(plan.slots),

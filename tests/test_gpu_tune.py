@@ -118,7 +118,9 @@ def test_every_fft_variant_matches_numpy(n):
     assert torch.equal(g, g2)
 
 
-def test_run_plan_matches_cover_plan():
+def test_plan_and_chunk_forms_agree():
+    """Cover and run plans, 64- and 32-voxel chunks: the same sums to the
+    split-BF16 accuracy."""
     from pyspectrum_gb300 import _lib, core
     from pyspectrum_gb300._lib import call, ptr, stream_ptr
     n, nmax = 48, 40
@@ -128,14 +130,16 @@ def test_run_plan_matches_cover_plan():
     T = slots.shape[1]
     tri_d = torch.from_numpy(slots).cuda()
     info = {}
-    for flags in (0, _lib.CONTRACT_RUN_PLAN):
-        v = np.zeros(8, dtype=np.int64)
-        call("pyspec_bk_plan_check_flags", nmax, slots.ctypes.data_as(ctypes.c_void_p), T, flags, v.ctypes.data, 8)
+    combos = (0, _lib.CONTRACT_KC32, _lib.CONTRACT_RUN_PLAN, _lib.CONTRACT_RUN_PLAN | _lib.CONTRACT_KC32)
+    for flags in combos:
+        v = np.zeros(9, dtype=np.int64)
+        call("pyspec_bk_plan_check_flags", nmax, slots.ctypes.data_as(ctypes.c_void_p), T, flags, v.ctypes.data, 9)
         info[flags] = v
     assert info[0][2] == 1 and info[_lib.CONTRACT_RUN_PLAN][2] == 0      # cover vs run plan
+    assert info[0][8] == 64 and info[_lib.CONTRACT_KC32][8] == 32        # 64- vs 32-voxel chunks
     out = {}
     lib = _lib.load()
-    for flags in (0, _lib.CONTRACT_RUN_PLAN):
+    for flags in combos:
         ws = torch.zeros(lib.pyspec_bk_contract_workspace(n, nmax, T, 1 | flags), dtype=torch.uint8, device="cuda")
         b = torch.zeros(T, dtype=torch.float64, device="cuda")
         call("pyspec_bk_contract", ptr(fields), n, nmax, ptr(tri_d), slots.ctypes.data_as(ctypes.c_void_p), T,
