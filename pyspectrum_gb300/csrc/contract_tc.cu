@@ -691,9 +691,13 @@ constexpr int ALO_TILE_BYTES = 128 * KC64 * 2;      // A_lo of one tile and stag
 constexpr int SEG64_SHIFT = 1;                       // drains every 2^(seg_log2 - 1) deep chunks (same voxels)
 constexpr int kDeepSmemLimit = 232448 - 6144;        // dynamic bytes: the 227 KB opt-in less the static arrays
 
+// A_lo blocks in shared memory: tiles 0 and 1 (tile 2 keeps its A_lo in
+// TMEM, in the columns of the absent tile 3)
+__host__ __device__ constexpr int alo_smem_tiles(int ntiles) { return ntiles < 2 ? ntiles : 2; }
+
 // dynamic shared memory before the Kahan slots, for nfbuf field buffers of two halves
 __host__ __device__ constexpr int fixed_smem64(int nshell, int ntiles, int nfbuf) {
-    return 1024 + nfbuf * 2 * f_bytes(nshell) + NSTAGE * STAGE64_BYTES + NSTAGE * ntiles * ALO_TILE_BYTES;
+    return 1024 + nfbuf * 2 * f_bytes(nshell) + NSTAGE * STAGE64_BYTES + NSTAGE * alo_smem_tiles(ntiles) * ALO_TILE_BYTES;
 }
 
 // K-major no-swizzle operand with 64 k per row block: core matrix (r/8, g) at
@@ -729,10 +733,28 @@ __device__ __forceinline__ void store_slot64(float4 fi, const float4* fj, uint32
     }
 }
 
+// store_slot64 for tile 2: the lo parts go to TMEM too (8 columns at `lo_addr`)
+__device__ __forceinline__ void store_slot64_tmem(float4 fi, const float4* fj, uint32_t addr, uint32_t lo_addr) {
+#pragma unroll
+    for (int blk = 0; blk < 2; ++blk) {
+        uint32_t h[4], l[4];
+#pragma unroll
+        for (int yy = 0; yy < 2; ++yy) {
+            const float4 f = fj[2 * blk + yy];
+            const float2 p0 = mul2(make_float2(fi.x, fi.y), make_float2(f.x, f.y));
+            const float2 p1 = mul2(make_float2(fi.z, fi.w), make_float2(f.z, f.w));
+            split2(p0, h[2 * yy], l[2 * yy]);
+            split2(p1, h[2 * yy + 1], l[2 * yy + 1]);
+        }
+        tmem_st16x256_x1(addr + ((uint32_t)(16 * blk) << 16), h);
+        tmem_st16x256_x1(lo_addr + ((uint32_t)(16 * blk) << 16), l);
+    }
+}
+
 // The MMAs of one deep chunk (all tiles wide): per k-step and tile, A_hi from
 // TMEM (`abase` + 32 t + 8 ks) and A_lo from shared memory (`alo0` + 16 KB t
-// + 256 ks) against the stage's B rows (`bd0` + 256 ks, 8-row blocks 1024
-// bytes apart).
+// + 256 ks; tile 2: from TMEM, `abase` + 32 * 3 + 8 ks) against the stage's
+// B rows (`bd0` + 256 ks, 8-row blocks 1024 bytes apart).
 template <int NT>
 __device__ __forceinline__ void issue_chunk64(const uint32_t (&dcol)[MAXTILES], uint32_t abase, uint64_t alo0,
                                               uint64_t bd0, const uint32_t (&idesc)[MAXTILES], uint32_t first) {
@@ -746,8 +768,12 @@ __device__ __forceinline__ void issue_chunk64(const uint32_t (&dcol)[MAXTILES], 
             const uint64_t alo = alo0 + (uint64_t)((t * ALO_TILE_BYTES + ks * 256) >> 4);
             asm volatile("{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n"
                          :: "r"(dcol[t]), "r"(ahi), "l"(bd), "r"(idesc[t]), "r"(acc0));
-            asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, 1;"
-                         :: "r"(dcol[t]), "l"(alo), "l"(bd), "r"(idesc[t]));
+            if (t < 2)
+                asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, 1;"
+                             :: "r"(dcol[t]), "l"(alo), "l"(bd), "r"(idesc[t]));
+            else
+                asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, 1;"
+                             :: "r"(dcol[t]), "r"(abase + (uint32_t)(3 * ACOLS + ks * 8)), "l"(bd), "r"(idesc[t]));
         }
     }
 }
@@ -771,8 +797,9 @@ contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ C
     unsigned char* stage_base = smem + NFB * 2 * F_BYTES;                    // NSTAGE x B operand
     __syncthreads();
     const int ntl = G.ntiles;
-    unsigned char* alo_base = stage_base + NSTAGE * STAGE64_BYTES;            // NSTAGE x ntiles x A_lo
-    float2* acc = reinterpret_cast<float2*>(alo_base + NSTAGE * ntl * ALO_TILE_BYTES);
+    const int nlo = alo_smem_tiles(ntl);
+    unsigned char* alo_base = stage_base + NSTAGE * STAGE64_BYTES;            // NSTAGE x nlo x A_lo
+    float2* acc = reinterpret_cast<float2*>(alo_base + NSTAGE * nlo * ALO_TILE_BYTES);
 
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
@@ -910,7 +937,7 @@ contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ C
             }
             const unsigned char* F = fbuf + (size_t)b * 2 * F_BYTES;
             char* Bst = reinterpret_cast<char*>(stage_base) + (size_t)s * STAGE64_BYTES;
-            char* Alo = reinterpret_cast<char*>(alo_base) + (size_t)s * ntl * ALO_TILE_BYTES;
+            char* Alo = reinterpret_cast<char*>(alo_base) + (size_t)s * nlo * ALO_TILE_BYTES;
             if (ub_r >= 0) {
                 const unsigned char* Fh = F + (ub_g >> 2) * F_BYTES;
                 const int g4 = ub_g & 3;
@@ -930,8 +957,10 @@ contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ C
                     float4 fj[4];
 #pragma unroll
                     for (int y = 0; y < 4; ++y) fj[y] = lds4(Fh, oj0[y]);
-                    store_slot64(fi0, fj, lane_base + acol(s, 2 * tp, ks),
-                                 Alo + (2 * tp) * ALO_TILE_BYTES + alo_thr + h * 512);
+                    if (tp == 0)
+                        store_slot64(fi0, fj, lane_base + acol(s, 0, ks), Alo + alo_thr + h * 512);
+                    else
+                        store_slot64_tmem(fi0, fj, lane_base + acol(s, 2, ks), lane_base + acol(s, 3, ks));
                     if (slot1_on) {
                         if (reload) {
 #pragma unroll
@@ -944,7 +973,7 @@ contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ C
             }
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
             // A_lo and B writes (generic proxy) made visible to the MMA (async proxy)
-            if (tp_on || b_warp) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            if ((tp_on && (tp == 0 || ntl == 2)) || b_warp) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
             if (lane == 0) {
@@ -978,7 +1007,7 @@ contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ C
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t abase = tmem + acol(s, 0, 0);
                 const uint64_t bd0 = bdesc0 + (uint64_t)((s * STAGE64_BYTES) >> 4);
-                const uint64_t alo0 = adesc0 + (uint64_t)((s * ntl * ALO_TILE_BYTES) >> 4);
+                const uint64_t alo0 = adesc0 + (uint64_t)((s * nlo * ALO_TILE_BYTES) >> 4);
                 if (ntl == 2) issue_chunk64<2>(dcol, abase, alo0, bd0, idesc, first);
                 else issue_chunk64<3>(dcol, abase, alo0, bd0, idesc, first);
                 first = 1u;
