@@ -1106,6 +1106,14 @@ static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 static std::mutex g_plan_mu;
 static std::map<std::vector<int32_t>, HostPlan*> g_plans;
 
+// Pads a group's Kahan-slot list so that row `row` (its index in the group)
+// starts its columns at a slot with (start - lmin) = row (mod 16): in a
+// drain the 16 lanes of a half-warp (16 consecutive rows) then update the
+// same column's slots in 16 different 8-byte bank pairs.
+static void align_row_slots(std::vector<int32_t>& v, int row, int lmin) {
+    while ((((int)v.size() - lmin - row) & 15) != 0) v.push_back(-1);
+}
+
 static int pow2_cols(int n) {
     int c = 32;
     while (c < n) c <<= 1;
@@ -1389,6 +1397,7 @@ static bool build_cover_plan(HostPlan* hp, int nshell, const int32_t* tri_host, 
         pr[0] = (int16_t)(R.f | (R.g << 8));
         pr[1] = (int16_t)lmin;
         pr[2] = (int16_t)lmax;
+        align_row_slots(gslots[0], r, lmin);
         pr[3] = (int16_t)gslots[0].size();
         size_t c = 0;
         for (int l = lmin; l <= lmax; ++l) {
@@ -1591,6 +1600,7 @@ static HostPlan* build_plan(int nshell, const int32_t* tri_host, int ntri, bool 
                         pr[0] = (int16_t)(i | (j << 8));
                         pr[1] = (int16_t)lmin;
                         pr[2] = (int16_t)lmax;
+                        align_row_slots(gslots[g], row, lmin);
                         pr[3] = (int16_t)gslots[g].size();
                         for (int l = lmin; l <= lmax; ++l) {
                             auto it = m.find(l);
