@@ -73,15 +73,16 @@ def job_rate(world, units_per_rank, seconds_max):
     return world * units_per_rank / seconds_max
 
 
-def plan_macs_per_voxel(nmax, ncut, step):
-    """Tensor-core multiply-adds per voxel of the contraction plan for the
-    triangle loop (host-side plan query of the library)."""
+def plan_info(nmax, ncut, step):
+    """Host-side plan query of the library for the triangle loop: tensor-core
+    multiply-adds per voxel of the contraction plan and its voxels per chunk
+    (64: contract_tc64_kernel, 32: contract_tc_kernel)."""
     from pyspectrum_gb300 import _lib, core as _core
     jmin = ncut // step
     tri = np.ascontiguousarray(_core.triangles(jmin, nmax) - jmin, dtype=np.int32)
-    info = np.zeros(7, dtype=np.int64)
-    _lib.call("pyspec_bk_plan_check", nmax - jmin + 1, tri.ctypes.data, int(tri.shape[1]), info.ctypes.data, 7)
-    return int(info[6])
+    info = np.zeros(9, dtype=np.int64)
+    _lib.call("pyspec_bk_plan_check", nmax - jmin + 1, tri.ctypes.data, int(tri.shape[1]), info.ctypes.data, 9)
+    return int(info[6]), int(info[8])
 
 
 def fp32_tiles(nmax, ncut, step):
@@ -460,9 +461,11 @@ def run_gpu(args, rank, world, local_rank):
     # library builds for this triangle list.
     V = n ** 3
     useful = 2.0 * plans["bf16x3"].T * V
-    executed = 2.0 * plan_macs_per_voxel(nmax, ncut, step) * V
+    macs, chunk = plan_info(nmax, ncut, step)
+    executed = 2.0 * macs * V
+    kname = "contract_tc64_kernel" if chunk == 64 else "contract_tc_kernel"
     t_con = main["stage_ms"]["contraction"] / 1e3
-    roofline = {"kernel": "contract_tc_kernel (+ partial reduction)", "bound": "tensor",
+    roofline = {"kernel": kname + " (+ partial reduction)", "bound": "tensor",
                 "achieved": useful / t_con / 1e12, "peak": bf16, "unit": "TFLOP/s",
                 "frac": useful / t_con / 1e12 / bf16, "peak_kind": kind,
                 "executed_tflops": executed / t_con / 1e12, "executed_frac": executed / t_con / 1e12 / bf16,
