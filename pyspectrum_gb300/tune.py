@@ -52,8 +52,19 @@ def cache_file() -> str:
     return os.path.join(core.cache_dir(), "tune.json")
 
 
+_dev_names: dict = {}
+
+
 def _device_key(device) -> str:
-    return torch.cuda.get_device_name(device).replace(" ", "_")
+    """Device name for cache keys, looked up once per device index (the
+    driver query costs more than the rest of a cached lookup)."""
+    d = torch.device(device) if not isinstance(device, int) else torch.device("cuda", device)
+    idx = d.index if d.index is not None else torch.cuda.current_device()
+    name = _dev_names.get(idx)
+    if name is None:
+        name = torch.cuda.get_device_name(idx).replace(" ", "_")
+        _dev_names[idx] = name
+    return name
 
 
 def _load():
@@ -101,12 +112,20 @@ def _time(fn, reps=REPS) -> float:
     return best
 
 
-def _pick(key, candidates, run):
-    """The stored choice for key, or the fastest candidate (timed with `run`)."""
+def _cached(key, candidates):
+    """The stored choice for key if it is one of the candidates, else None."""
     _load()
     got = _mem.get(key)
-    if got is not None and got.get("choice") in [c for c in candidates]:
+    if got is not None and got.get("choice") in candidates:
         return got["choice"]
+    return None
+
+
+def _pick(key, candidates, run):
+    """The stored choice for key, or the fastest candidate (timed with `run`)."""
+    got = _cached(key, candidates)
+    if got is not None:
+        return got
     times = {}
     for c in candidates:
         try:
@@ -161,18 +180,21 @@ def assign(xyzs, ws, n, kf_ks, offset, grid):
     if npart == 0:
         return ASSIGN_DEFAULT
     cands = assign_candidates(n)
-    wsbuf = {int(c[5:]): _assign_workspace(npart, n, int(c[5:]), dev) for c in cands if c != "direct"}
     if not enabled():
         choice = ASSIGN_DEFAULT
     else:
         density = npart / float(n) ** 3
         key = f"assign|{_device_key(dev)}|n{n}|ppc2^{int(round(math.log2(max(density, 1e-9))))}"
+        choice = _cached(key, cands)
+        if choice is None:                 # tune: every candidate on the same grid, zeroed before each
+            wsbuf = {int(c[5:]): _assign_workspace(npart, n, int(c[5:]), dev) for c in cands if c != "direct"}
 
-        def run(c):
+            def run(c):
+                grid.zero_()
+                _assign_run(c, xyzs, ws, n, kf_ks, offset, grid, wsbuf)
+            choice = _pick(key, cands, run)
             grid.zero_()
-            _assign_run(c, xyzs, ws, n, kf_ks, offset, grid, wsbuf)
-        choice = _pick(key, cands, run)
-        grid.zero_()
+    wsbuf = {} if choice == "direct" else {int(choice[5:]): _assign_workspace(npart, n, int(choice[5:]), dev)}
     _assign_run(choice, xyzs, ws, n, kf_ks, offset, grid, wsbuf)
     return choice
 
