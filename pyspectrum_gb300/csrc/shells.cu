@@ -350,8 +350,9 @@ __global__ void __launch_bounds__(256) shell_xpass_kernel(const typename cplx_t<
 // x rows for the common grid sizes, with the half-length FFT of H = R1*R2
 // points done in registers: a warp transforms two rows at a time (16 lanes
 // per row).  The next pair of rows is copied into a per-warp staging buffer
-// with cp.async while the current pair is transformed, so the row loads are
-// always in flight.  Stage 1 reads its inputs from the staging buffer, forms
+// by two bulk copies (TMA, cp.async.bulk: one per row, issued by lane 0,
+// completing on the warp's barrier of that stage) while the current pair is
+// transformed, so the row loads are always in flight.  Stage 1 reads its inputs from the staging buffer, forms
 // Z[k] (the C2R packing above) and applies radix-R1 butterflies; the outputs
 // cross lanes once through a padded per-row buffer in shared memory (one pad
 // element per R1, so neither side has bank conflicts); stage 2 applies the
@@ -373,10 +374,16 @@ __global__ void __launch_bounds__(256, 3) shell_xpass_reg_kernel(const float2* _
     __shared__ float2 twH[H];                    // exp(-2 pi i m / H)
     __shared__ float2 rowbuf[8][2][PADH];
     __shared__ double red[8];
+    __shared__ __align__(8) uint64_t stg_bar[8][2];        // per warp and stage: its two rows' bulk copies
     extern __shared__ __align__(16) float2 stage_all[];   // [warp][stage][row][WS]
     for (int i = threadIdx.x; i < H; i += blockDim.x) {
         twN[i] = twg[i];
         twH[i] = twg[N + i];
+    }
+    if (threadIdx.x < 16) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;"
+                     :: "r"((uint32_t)__cvta_generic_to_shared(&stg_bar[threadIdx.x >> 1][threadIdx.x & 1])), "r"(1));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -385,19 +392,50 @@ __global__ void __launch_bounds__(256, 3) shell_xpass_reg_kernel(const float2* _
     float2* stg = stage_all + (size_t)warp * 2 * 2 * WS;
     const int64_t nrows = (int64_t)N * N;        // even: rows come in pairs
     const int64_t nw = (int64_t)gridDim.x * 8;
-    // 16-byte pieces of a row holding its first xlim elements
-    const int npiece = (xlim + 1) / 2;
-    // copy the two rows starting at r0 into stage sb (every lane commits one group)
+    // the first xlim elements of a row in 16-byte pieces (rows start on
+    // 16-byte boundaries: the work-grid stride is a multiple of 8 elements)
+    const uint32_t row_bytes = (uint32_t)((xlim + 1) / 2) * 16u;
+    const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(&stg_bar[warp][0]);
+    // one bulk copy (TMA) per row of the pair starting at r0 into stage sb,
+    // completing on the warp's barrier of that stage; lane 0 issues them
+    // after the warp's reads of the stage (fenced against the async proxy)
+    uint32_t pending = 0u, phase = 0u;   // bit sb: stage sb has a copy in flight / its next parity
     auto issue = [&](int64_t r0, int sb) {
-        if (r0 < nrows) {
-            for (int q = lane; q < 2 * npiece; q += 32) {
-                const int rr = q >= npiece, pc = q - rr * npiece;
-                const float2* src = work + (r0 + rr) * WS + 2 * pc;
-                const uint32_t dst = (uint32_t)__cvta_generic_to_shared(stg + ((size_t)sb * 2 + rr) * WS + 2 * pc);
-                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" :: "r"(dst), "l"(src) : "memory");
+        if (r0 >= nrows) return;
+        pending |= 1u << sb;
+        if (lane == 0) {
+            const uint32_t bar = bar0 + 8u * (uint32_t)sb;
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(2u * row_bytes)
+                         : "memory");
+#pragma unroll
+            for (int rr = 0; rr < 2; ++rr) {
+                const uint32_t dst = (uint32_t)__cvta_generic_to_shared(stg + ((size_t)sb * 2 + rr) * WS);
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                    :: "r"(dst), "l"(work + (r0 + rr) * WS), "r"(row_bytes), "r"(bar) : "memory");
             }
         }
-        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    // all lanes wait for stage sb (bounded: ~2 s, then false)
+    auto wait_stage = [&](int sb) -> bool {
+        const uint32_t bar = bar0 + 8u * (uint32_t)sb;
+        uint32_t ok = 0;
+        unsigned long long t0 = 0;
+        for (uint32_t it = 0;; ++it) {
+            asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+                         : "=r"(ok) : "r"(bar), "r"((phase >> sb) & 1u) : "memory");
+            if (ok) break;
+            if ((it & 255u) == 0) {
+                unsigned long long t;
+                asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+                if (t0 == 0) t0 = t;
+                else if (t - t0 > 2000000000ull) return false;
+            }
+        }
+        phase ^= 1u << sb;
+        pending &= ~(1u << sb);
+        return true;
     };
     float local = 0.f;
     int sb = 0;
@@ -405,8 +443,10 @@ __global__ void __launch_bounds__(256, 3) shell_xpass_reg_kernel(const float2* _
     issue(r0, 0);
     for (; r0 < nrows; r0 += nw * 2, sb ^= 1) {
         issue(r0 + nw * 2, sb ^ 1);
-        asm volatile("cp.async.wait_group 1;" ::: "memory");
-        __syncwarp();                         // every lane's pieces of this pair have landed
+        if (!__all_sync(0xffffffffu, wait_stage(sb))) {
+            local = __int_as_float(0x7fc00000);   // NaN: the shell's sum of squares reports the failure
+            break;
+        }
         const int64_t row = r0 + sub;
         const float2* X = stg + ((size_t)sb * 2 + sub) * WS;
         if (t < R2) {
@@ -444,7 +484,9 @@ __global__ void __launch_bounds__(256, 3) shell_xpass_reg_kernel(const float2* _
         }
         __syncwarp();                         // buf and this stage are rewritten later
     }
-    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    // no copy may land after the CTA exits: wait (bounded) for any in flight
+    for (int k = 0; k < 2; ++k)
+        if ((pending >> k) & 1u) (void)__all_sync(0xffffffffu, wait_stage(k));
     double acc = (double)local;
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) red[warp] = acc;
