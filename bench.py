@@ -506,7 +506,7 @@ def run_gpu(args, rank, world, local_rank):
             "gpu_launches": main["gpu_launches"], "clocks": main["clocks"], "fft3d_comparator": fftcmp}
     from pyspectrum_gb300 import tune
     line["tuned"] = {k.split("|", 2)[0] + "|" + k.split("|", 2)[2]: v for k, v in tune.choices().items()
-                     if f"|n{n}|" in k}
+                     if f"|n{n}|" in k or k.endswith(f"|n{n}")}
     if not args.no_batch:
         try:
             line["batch_64_mocks"] = batch_rate()
