@@ -102,6 +102,29 @@ def test_arbitrary_triangle_lists():
         assert (np.abs(got - ref) / mag).max() < tol, method
 
 
+@pytest.mark.parametrize("n,nmax", [(30, 12), (50, 30), (18, 12)])
+def test_chunk_tails(n, nmax):
+    """Voxel counts that are not a multiple of 64 (N = 30, 50, 18: the last
+    64-voxel chunk is partly past the end and the copies fill it with zeros;
+    N = 50, Nmax 30 also has empty shells past the Nyquist shell) and grids
+    with fewer chunks than CTAs (N = 18, 30): the 64- and 32-voxel
+    tensor-core forms against float64."""
+    jmin = 1
+    fields = _fields(n, 1, jmin, nmax, seed=n)
+    slots = np.ascontiguousarray(core.triangles(jmin, nmax) - jmin, dtype=np.int32)
+    info = np.zeros(9, dtype=np.int64)
+    call("pyspec_bk_plan_check", nmax, slots.ctypes.data_as(ctypes.c_void_p), slots.shape[1],
+         info.ctypes.data_as(ctypes.c_void_p), 9)
+    assert info[8] == 64
+    ref, mag = _reference(fields, slots)
+    mag = np.maximum(mag, 1e-300)
+    for flags in (0, 0x400):                 # 64-voxel chunks, then PYSPEC_CONTRACT_KC32
+        got, status = _contract(fields, n, slots, 1 | flags)
+        assert status == 0
+        err = np.abs(got - ref) / mag
+        assert err.max() < 3e-5 and np.median(err) < 3e-6, flags
+
+
 def test_cover_plan_narrow_three_tiles():
     """The Nmax 40 loop moved to shells 7..46 of 48: its pair cover still fits
     3 tiles, but columns up to 46 exceed the wide form's TMEM budget, so the
