@@ -271,13 +271,29 @@ class BkPlan:
         method: 0, or the code of a bounded wait that timed out)."""
         return self.ws_con[:4].view(torch.int32)
 
+    def _readback(self):
+        """The output arrays and the contraction's status word, copied to
+        page-locked host buffers on the current stream and read after one
+        synchronisation (status 0 for the FP32 method)."""
+        tensor = self.method in TENSOR_METHODS
+        if self.out.device.type != "cuda":          # host-side buffers (plan logic without a device)
+            return self.out.numpy().copy(), int(self.status_word()[0]) if tensor else 0
+        if getattr(self, "_host_out", None) is None:
+            self._host_out = torch.empty(tuple(self.out.shape), dtype=torch.float64).pin_memory()
+            self._host_status = torch.zeros(1, dtype=torch.int32).pin_memory()
+        self._host_out.copy_(self.out, non_blocking=True)
+        if tensor:
+            self._host_status.copy_(self.status_word(), non_blocking=True)
+        torch.cuda.current_stream(self.out.device).synchronize()
+        return self._host_out.numpy().copy(), int(self._host_status[0]) if tensor else 0
+
     def result(self, apply_units=False):
         """Copy the normalised arrays to the host as the reference's output dict.
         Only triangles with counts > 0 are returned (all arrays aligned).
         Raises ContractTimeout if the tensor-core contraction stopped early."""
-        out = self.out.cpu().numpy()
+        out, status = self._readback()
         if self.method in TENSOR_METHODS:
-            check_contract_status(self.status_word().item())
+            check_contract_status(status)
         keep = self.counts_np > 0
         tri = self.tri_np[:, keep]
         res = {
