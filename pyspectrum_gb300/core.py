@@ -285,7 +285,7 @@ class BkPlan:
         if tensor:
             self._host_status.copy_(self.status_word(), non_blocking=True)
         torch.cuda.current_stream(self.out.device).synchronize()
-        return self._host_out.numpy().copy(), int(self._host_status[0]) if tensor else 0
+        return self._host_out.numpy(), int(self._host_status[0]) if tensor else 0
 
     def result(self, apply_units=False):
         """Copy the normalised arrays to the host as the reference's output dict.
@@ -294,17 +294,18 @@ class BkPlan:
         out, status = self._readback()
         if self.method in TENSOR_METHODS:
             check_contract_status(status)
-        keep = self.counts_np > 0
-        tri = self.tri_np[:, keep]
+        if getattr(self, "_keep", None) is None:      # the kept triangles and their k indices, once per plan
+            self._keep = np.nonzero(self.counts_np > 0)[0]
+            self._ik = self.tri_np[:, self._keep].astype(np.int64) * self.step
+        # every triangle kept (the usual case at the common grid sizes): one copy
+        o = out.copy() if len(self._keep) == out.shape[1] else np.take(out, self._keep, axis=1)
         res = {
-            "i_k1": tri[0].astype(np.int64) * self.step,
-            "i_k2": tri[1].astype(np.int64) * self.step,
-            "i_k3": tri[2].astype(np.int64) * self.step,
-            "p0k1": out[0, keep], "p0k2": out[1, keep], "p0k3": out[2, keep],
-            "b123": out[3, keep], "q123": out[4, keep], "counts": out[5, keep],
+            "i_k1": self._ik[0].copy(), "i_k2": self._ik[1].copy(), "i_k3": self._ik[2].copy(),
+            "p0k1": o[0], "p0k2": o[1], "p0k3": o[2],
+            "b123": o[3], "q123": o[4], "counts": o[5],
         }
         if apply_units:
-            res["b123_sn"] = out[6, keep]
+            res["b123_sn"] = o[6]
         return res
 
 
