@@ -136,44 +136,83 @@ __global__ void __launch_bounds__(kThreads) tile_accum_kernel(const float* __res
     const int ox = tx * B, oy = ty * B, oz = tz * B;   // first cell of the block (before wrap)
     for (int k = threadIdx.x; k < E * E * E; k += blockDim.x) blk[k] = make_float2(0.f, 0.f);
     __syncthreads();
-    for (int k = p0 + threadIdx.x; k < p1; k += blockDim.x) {
-        const int64_t i = order[k];
+    const int o[3] = {ox, oy, oz};
+    if ((p1 - p0) * 8 > 4 * (int)blockDim.x) {
+        // dense tile: one thread per particle, both grids and all 64 cells
+        for (int k = p0 + threadIdx.x; k < p1; k += blockDim.x) {
+            const int64_t i = order[k];
+            const float we = w ? w[i] : 1.0f;
+            int base[2][3];
+            float wt[2][3][4];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const float r = xyz[d * np + i];
+                const float rx = __fadd_rn(__fadd_rn(__fmul_rn(kf_ks, r), 1.0f), offset);   // estimator.f:302
+                const float tq = __fadd_rn(rx, 0.5f);                                      // estimator.f:305
+                const int m = __float2int_rz(rx);
+                const int q = __float2int_rz(tq);
+                pcs_w(__fsub_rn(rx, (float)m), wt[0][d]);
+                pcs_w(__fsub_rn(tq, (float)q), wt[1][d]);
+                base[0][d] = m;
+                base[1][d] = q;
+            }
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                int lc[3][4];                            // block-local cells per axis, in [0, E)
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) lc[d][c] = wrapi(base[s][d] - 2 + c - o[d], n);
+#pragma unroll
+                for (int c3 = 0; c3 < 4; ++c3)
+#pragma unroll
+                    for (int c2 = 0; c2 < 4; ++c2) {
+                        float* row = reinterpret_cast<float*>(blk + (lc[2][c3] * E + lc[1][c2]) * E) + s;
+#pragma unroll
+                        for (int c1 = 0; c1 < 4; ++c1) {
+                            // estimator.f:380: ((hx*hy)*hz)*we
+                            const float v = __fmul_rn(__fmul_rn(__fmul_rn(wt[s][0][c1], wt[s][1][c2]), wt[s][2][c3]), we);
+                            atomicAdd(row + 2 * lc[0][c1], v);
+                        }
+                    }
+            }
+        }
+    } else {
+    // sparse tile: eight work items per particle, (grid s, z offset c3), each
+    // adding its 4 x 4 weights (short atomic chains, and the CTA's threads
+    // stay busy when the tile holds fewer particles than threads)
+    for (int it = threadIdx.x; it < (p1 - p0) * 8; it += blockDim.x) {
+        const int64_t i = order[p0 + (it >> 3)];
+        const int s = (it >> 2) & 1, c3 = it & 3;
         const float we = w ? w[i] : 1.0f;
-        int base[2][3];
-        float wt[2][3][4];
+        int base[3];
+        float wt[3][4];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const float r = xyz[d * np + i];
             const float rx = __fadd_rn(__fadd_rn(__fmul_rn(kf_ks, r), 1.0f), offset);   // estimator.f:302
-            const float tq = __fadd_rn(rx, 0.5f);                                      // estimator.f:305
-            const int m = __float2int_rz(rx);
-            const int q = __float2int_rz(tq);
-            pcs_w(__fsub_rn(rx, (float)m), wt[0][d]);
-            pcs_w(__fsub_rn(tq, (float)q), wt[1][d]);
-            base[0][d] = m;
-            base[1][d] = q;
+            const float tq = s ? __fadd_rn(rx, 0.5f) : rx;                             // estimator.f:305
+            const int m = __float2int_rz(tq);
+            pcs_w(__fsub_rn(tq, (float)m), wt[d]);
+            base[d] = m;
         }
-        const int o[3] = {ox, oy, oz};
+        int lc[2][4];                                // block-local cells along x and y, in [0, E)
 #pragma unroll
-        for (int s = 0; s < 2; ++s) {
-            int lc[3][4];                            // block-local cells per axis, in [0, E)
+        for (int d = 0; d < 2; ++d)
 #pragma unroll
-            for (int d = 0; d < 3; ++d)
+            for (int c = 0; c < 4; ++c) lc[d][c] = wrapi(base[d] - 2 + c - o[d], n);
+        const int lz = wrapi(base[2] - 2 + c3 - o[2], n);
 #pragma unroll
-                for (int c = 0; c < 4; ++c) lc[d][c] = wrapi(base[s][d] - 2 + c - o[d], n);
+        for (int c2 = 0; c2 < 4; ++c2) {
+            float* row = reinterpret_cast<float*>(blk + (lz * E + lc[1][c2]) * E) + s;
 #pragma unroll
-            for (int c3 = 0; c3 < 4; ++c3)
-#pragma unroll
-                for (int c2 = 0; c2 < 4; ++c2) {
-                    float* row = reinterpret_cast<float*>(blk + (lc[2][c3] * E + lc[1][c2]) * E) + s;
-#pragma unroll
-                    for (int c1 = 0; c1 < 4; ++c1) {
-                        // estimator.f:380: ((hx*hy)*hz)*we
-                        const float v = __fmul_rn(__fmul_rn(__fmul_rn(wt[s][0][c1], wt[s][1][c2]), wt[s][2][c3]), we);
-                        atomicAdd(row + 2 * lc[0][c1], v);
-                    }
-                }
+            for (int c1 = 0; c1 < 4; ++c1) {
+                // estimator.f:380: ((hx*hy)*hz)*we
+                const float v = __fmul_rn(__fmul_rn(__fmul_rn(wt[0][c1], wt[1][c2]), wt[2][c3]), we);
+                atomicAdd(row + 2 * lc[0][c1], v);
+            }
         }
+    }
     }
     __syncthreads();
     for (int k = threadIdx.x; k < E * E * E; k += blockDim.x) {
@@ -182,8 +221,8 @@ __global__ void __launch_bounds__(kThreads) tile_accum_kernel(const float* __res
         const int lx = k % E, ly = (k / E) % E, lz = k / (E * E);
         const int gx = wrapi(ox + lx, n), gy = wrapi(oy + ly, n), gz = wrapi(oz + lz, n);
         float* g = grid + 2 * (((int64_t)gz * n + gy) * n + gx);
-        if (v.x != 0.f) atomicAdd(g, v.x);
-        if (v.y != 0.f) atomicAdd(g + 1, v.y);
+        // both grids of the cell with one 8-byte vector reduction
+        asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" :: "l"(g), "f"(v.x), "f"(v.y) : "memory");
     }
 }
 
