@@ -714,6 +714,9 @@ __device__ __forceinline__ void tmem_st16x256_x1(uint32_t addr, const uint32_t* 
 // rows into TMEM (lanes x + 8y of the quarter, 8 columns at `addr`), the lo
 // parts into the tile's A_lo block (`alo` = this thread's address for row
 // y = 0; row y lies in the next 8-row block, y * 1024 bytes further).
+// RES (the residual pass of the 6-product form): the third parts take the
+// place of the lo parts.
+template <bool RES = false>
 __device__ __forceinline__ void store_slot64(float4 fi, const float4* fj, uint32_t addr, char* alo) {
 #pragma unroll
     for (int blk = 0; blk < 2; ++blk) {
@@ -723,8 +726,13 @@ __device__ __forceinline__ void store_slot64(float4 fi, const float4* fj, uint32
             const float4 f = fj[2 * blk + yy];
             const float2 p0 = mul2(make_float2(fi.x, fi.y), make_float2(f.x, f.y));
             const float2 p1 = mul2(make_float2(fi.z, fi.w), make_float2(f.z, f.w));
-            split2(p0, h[2 * yy], l[2 * yy]);
-            split2(p1, h[2 * yy + 1], l[2 * yy + 1]);
+            if constexpr (RES) {
+                split2_res(p0, h[2 * yy], l[2 * yy]);
+                split2_res(p1, h[2 * yy + 1], l[2 * yy + 1]);
+            } else {
+                split2(p0, h[2 * yy], l[2 * yy]);
+                split2(p1, h[2 * yy + 1], l[2 * yy + 1]);
+            }
         }
         tmem_st16x256_x1(addr + ((uint32_t)(16 * blk) << 16), h);
         // rows y = 2 blk and 2 blk + 1 sit in 8-row blocks 2 blk and 2 blk + 1 of the quarter
@@ -734,6 +742,7 @@ __device__ __forceinline__ void store_slot64(float4 fi, const float4* fj, uint32
 }
 
 // store_slot64 for tile 2: the lo parts go to TMEM too (8 columns at `lo_addr`)
+template <bool RES = false>
 __device__ __forceinline__ void store_slot64_tmem(float4 fi, const float4* fj, uint32_t addr, uint32_t lo_addr) {
 #pragma unroll
     for (int blk = 0; blk < 2; ++blk) {
@@ -743,8 +752,13 @@ __device__ __forceinline__ void store_slot64_tmem(float4 fi, const float4* fj, u
             const float4 f = fj[2 * blk + yy];
             const float2 p0 = mul2(make_float2(fi.x, fi.y), make_float2(f.x, f.y));
             const float2 p1 = mul2(make_float2(fi.z, fi.w), make_float2(f.z, f.w));
-            split2(p0, h[2 * yy], l[2 * yy]);
-            split2(p1, h[2 * yy + 1], l[2 * yy + 1]);
+            if constexpr (RES) {
+                split2_res(p0, h[2 * yy], l[2 * yy]);
+                split2_res(p1, h[2 * yy + 1], l[2 * yy + 1]);
+            } else {
+                split2(p0, h[2 * yy], l[2 * yy]);
+                split2(p1, h[2 * yy + 1], l[2 * yy + 1]);
+            }
         }
         tmem_st16x256_x1(addr + ((uint32_t)(16 * blk) << 16), h);
         tmem_st16x256_x1(lo_addr + ((uint32_t)(16 * blk) << 16), l);
@@ -755,7 +769,11 @@ __device__ __forceinline__ void store_slot64_tmem(float4 fi, const float4* fj, u
 // TMEM (`abase` + 32 t + 8 ks) and A_lo from shared memory (`alo0` + 16 KB t
 // + 256 ks; tile 2: from TMEM, `abase` + 32 * 3 + 8 ks) against the stage's
 // B rows (`bd0` + 256 ks, 8-row blocks 1024 bytes apart).
-template <int NT>
+// RES (the residual pass, narrow accumulators): per tile and k-step A_res
+// (where A_lo would be) against the B_hi blocks (`bd0` then describes the hi
+// blocks only, 2048 bytes apart), and A_hi against the B_res blocks (1024
+// bytes further).
+template <int NT, bool RES = false>
 __device__ __forceinline__ void issue_chunk64(const uint32_t (&dcol)[MAXTILES], uint32_t abase, uint64_t alo0,
                                               uint64_t bd0, const uint32_t (&idesc)[MAXTILES], uint32_t first) {
 #pragma unroll
@@ -766,6 +784,18 @@ __device__ __forceinline__ void issue_chunk64(const uint32_t (&dcol)[MAXTILES], 
         for (int t = 0; t < NT; ++t) {
             const uint32_t ahi = abase + (uint32_t)(t * ACOLS + ks * 8);
             const uint64_t alo = alo0 + (uint64_t)((t * ALO_TILE_BYTES + ks * 256) >> 4);
+            if constexpr (RES) {
+                if (t < 2)
+                    asm volatile("{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                                 :: "r"(dcol[t]), "l"(alo), "l"(bd), "r"(idesc[t]), "r"(acc0));
+                else
+                    asm volatile("{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n"
+                                 :: "r"(dcol[t]), "r"(abase + (uint32_t)(3 * ACOLS + ks * 8)), "l"(bd), "r"(idesc[t]),
+                                    "r"(acc0));
+                asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, 1;"
+                             :: "r"(dcol[t]), "r"(ahi), "l"(bd + (uint64_t)(1024 >> 4)), "r"(idesc[t]));
+                continue;
+            }
             asm volatile("{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n"
                          :: "r"(dcol[t]), "r"(ahi), "l"(bd), "r"(idesc[t]), "r"(acc0));
             if (t < 2)
@@ -778,9 +808,10 @@ __device__ __forceinline__ void issue_chunk64(const uint32_t (&dcol)[MAXTILES], 
     }
 }
 
-template <int NFB>
+template <int NFB, bool RES = false>
 __global__ void __launch_bounds__(NTHREADS, 1)
 contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ CUtensorMap fmap) {
+    // RES: the residual pass of the 6-product form (narrow accumulators)
     extern __shared__ unsigned char smem_raw[];
     __shared__ Group G;
     __shared__ __align__(8) uint64_t bar_full[NSTAGE], bar_empty[NSTAGE], bar_ffull[NFB], bar_fempty[NFB];
@@ -807,7 +838,7 @@ contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ C
     const int64_t c1 = min(P.nchunks, c0 + P.chunks_per_cta);
     const int nch = (int)max((int64_t)0, c1 - c0);
     int C = 0;
-    for (int t = 0; t < ntl; ++t) C = max(C, G.tile_col[t] + 2 * G.tile_n[t]);
+    for (int t = 0; t < ntl; ++t) C = max(C, G.tile_col[t] + (RES ? 1 : 2) * G.tile_n[t]);
 
     for (int i = tid; i < MAXROWS * 4; i += NTHREADS) pij[i] = P.pair_row[(size_t)G.table_off * 4 + i];
     for (int i = tid; i < G.nslots; i += NTHREADS) acc[i] = make_float2(0.f, 0.f);
@@ -897,13 +928,14 @@ contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ C
                 const int drow = 128 * t + 32 * q + lane;
                 const short4 pr = drow < rows ? *reinterpret_cast<const short4*>(&pij[4 * drow])
                                               : make_short4(-1, 0, -1, 0);
-                const int sh0 = (cg - G.tile_col[t]) >> 1;
+                // wide: the hi and lo columns of 8 shells; narrow (RES): 16 shells
+                const int sh0 = RES ? cg - G.tile_col[t] : (cg - G.tile_col[t]) >> 1;
 #pragma unroll
-                for (int e = 0; e < 8; ++e) {
+                for (int e = 0; e < (RES ? 16 : 8); ++e) {
                     const int l = sh0 + e;
                     if (pr.x < 0 || l < pr.y || l > pr.z) continue;
                     const int slot = pr.w + (l - pr.y);
-                    const float v = __uint_as_float(d[e]) + __uint_as_float(d[e + 8]);
+                    const float v = RES ? __uint_as_float(d[e]) : __uint_as_float(d[e]) + __uint_as_float(d[e + 8]);
                     const float2 a = acc[slot];
                     const float y = v - a.y;
                     const float sum = a.x + y;
@@ -945,7 +977,8 @@ contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ C
                 const float4 e = *reinterpret_cast<const float4*>(Fh + fchunk(ub_r, 2 * g4 + 1));
                 const float2 x[4] = {make_float2(a.x, a.y), make_float2(a.z, a.w), make_float2(e.x, e.y),
                                      make_float2(e.z, e.w)};
-                split_store8(x, Bst + op_off64(brow(ub_r, 0), ub_g), Bst + op_off64(brow(ub_r, 1), ub_g));
+                if constexpr (RES) split_store8_res(x, Bst + op_off64(brow(ub_r, 0), ub_g), Bst + op_off64(brow(ub_r, 1), ub_g));
+                else split_store8(x, Bst + op_off64(brow(ub_r, 0), ub_g), Bst + op_off64(brow(ub_r, 1), ub_g));
             }
             if (tp_on) {
 #pragma unroll
@@ -958,15 +991,15 @@ contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ C
 #pragma unroll
                     for (int y = 0; y < 4; ++y) fj[y] = lds4(Fh, oj0[y]);
                     if (tp == 0)
-                        store_slot64(fi0, fj, lane_base + acol(s, 0, ks), Alo + alo_thr + h * 512);
+                        store_slot64<RES>(fi0, fj, lane_base + acol(s, 0, ks), Alo + alo_thr + h * 512);
                     else
-                        store_slot64_tmem(fi0, fj, lane_base + acol(s, 2, ks), lane_base + acol(s, 3, ks));
+                        store_slot64_tmem<RES>(fi0, fj, lane_base + acol(s, 2, ks), lane_base + acol(s, 3, ks));
                     if (slot1_on) {
                         if (reload) {
 #pragma unroll
                             for (int y = 0; y < 4; ++y) fj[y] = lds4(Fh, foff((int)((gs1 >> (8 * y)) & 0xffu)));
                         }
-                        store_slot64(fi1, fj, lane_base + acol(s, 2 * tp + 1, ks),
+                        store_slot64<RES>(fi1, fj, lane_base + acol(s, 2 * tp + 1, ks),
                                      Alo + (2 * tp + 1) * ALO_TILE_BYTES + alo_thr + h * 512);
                     }
                 }
@@ -993,10 +1026,11 @@ contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ C
             uint32_t idesc[MAXTILES], dcol[MAXTILES];
 #pragma unroll
             for (int t = 0; t < MAXTILES; ++t) {
-                idesc[t] = make_idesc(128, 2 * G.tile_n[t]);
+                idesc[t] = make_idesc(128, (RES ? 1 : 2) * G.tile_n[t]);
                 dcol[t] = tmem + (uint32_t)G.tile_col[t];
             }
-            const uint64_t bdesc0 = make_desc(smem_u32(stage_base), 128, 1024);
+            // all B rows (wide), or the hi blocks only (RES: 2048 bytes apart)
+            const uint64_t bdesc0 = make_desc(smem_u32(stage_base), 128, RES ? 2048 : 1024);
             const uint64_t adesc0 = make_desc(smem_u32(alo_base), 128, 1024);
             int seg_count = 0;
             const int seg_mask = (1 << seg_log2) - 1;
@@ -1008,8 +1042,8 @@ contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ C
                 const uint32_t abase = tmem + acol(s, 0, 0);
                 const uint64_t bd0 = bdesc0 + (uint64_t)((s * STAGE64_BYTES) >> 4);
                 const uint64_t alo0 = adesc0 + (uint64_t)((s * nlo * ALO_TILE_BYTES) >> 4);
-                if (ntl == 2) issue_chunk64<2>(dcol, abase, alo0, bd0, idesc, first);
-                else issue_chunk64<3>(dcol, abase, alo0, bd0, idesc, first);
+                if (ntl == 2) issue_chunk64<2, RES>(dcol, abase, alo0, bd0, idesc, first);
+                else issue_chunk64<3, RES>(dcol, abase, alo0, bd0, idesc, first);
                 first = 1u;
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                              :: "r"(smem_u32(&bar_empty[s])) : "memory");
@@ -1802,8 +1836,21 @@ int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_
             G.wide = 0;
             G.ncols = pow2_cols(col + NSTAGE * MAXTILES * ACOLS);
         }
-        PYSPEC_TRY(allow_smem((const void*)contract_tc_kernel<true>, hp->smem));
-        contract_tc_kernel<true><<<dim3(gx, R.ngroups), NTHREADS, hp->smem, st>>>(R, fmap);
+        if (hp->nfb64 > 0 && !kc32) {
+            // 64-voxel chunks for this pass too
+            R.nchunks = (nvox + KC64 - 1) / KC64;
+            R.chunks_per_cta = (R.nchunks + gx - 1) / gx;
+            const void* fn = hp->nfb64 == 3 ? (const void*)contract_tc64_kernel<3, true>
+                                            : (const void*)contract_tc64_kernel<2, true>;
+            PYSPEC_TRY(allow_smem(fn, hp->smem64));
+            if (hp->nfb64 == 3)
+                contract_tc64_kernel<3, true><<<dim3(gx, R.ngroups), NTHREADS, hp->smem64, st>>>(R, fmap);
+            else
+                contract_tc64_kernel<2, true><<<dim3(gx, R.ngroups), NTHREADS, hp->smem64, st>>>(R, fmap);
+        } else {
+            PYSPEC_TRY(allow_smem((const void*)contract_tc_kernel<true>, hp->smem));
+            contract_tc_kernel<true><<<dim3(gx, R.ngroups), NTHREADS, hp->smem, st>>>(R, fmap);
+        }
         PYSPEC_LAUNCH_CHECK();
         count_launch();
     }
