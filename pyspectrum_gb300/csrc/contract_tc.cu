@@ -875,38 +875,41 @@ contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ C
 
     if (warp < PWARPS) {
         // ================= producers =================
-        // As in the 32-voxel kernel, warp w owns TMEM lane quarter w % 4 of
-        // tile pair (w / 4) % 2; it forms k-steps (w / 8) % 2 and (w / 8) % 2
-        // + 2 of each chunk (the same 16-voxel position in both 32-voxel halves).
+        // Warp w owns TMEM lane quarter w % 4 and forms k-step w / 4 (0..3)
+        // of every chunk for all tiles: the row thread of tile pair 0
+        // (tiles 0 and 1, A_lo in shared memory) and, with three tiles, that
+        // of tile pair 1 (tile 2, A_lo in TMEM) -- the same work for every
+        // warp.  k-steps 0, 1 lie in the first 32-voxel half, 2, 3 in the second.
         const int rows = G.rows;
         const int nsh = P.nshell;
-        const int tp = (warp >> 2) & 1;
-        const int kstep = (warp >> 3) & 1;
-        const uint32_t kx = kstep ? 64u : 0u;
-        const bool tp_on = 2 * tp < ntl;
-        const bool slot1_on = 2 * tp + 1 < ntl;
+        const int ks = warp >> 2;
+        const int hh = ks >> 1;
+        const uint32_t kx = (ks & 1) ? 64u : 0u;
+        const bool b_on = ntl > 2;
         const int ax = lane & 3;
         const int xr = lane >> 2;
-        const int32_t* rtw = P.rt_tab + ((size_t)blockIdx.y * RT_PER_GROUP + tp * 32 + q * 8 + xr) * RT_WORDS;
-        const uint32_t code = (uint32_t)rtw[0];
-        const uint32_t gs0 = (uint32_t)rtw[1], gs1 = (uint32_t)rtw[2];
+        const int32_t* rta = P.rt_tab + ((size_t)blockIdx.y * RT_PER_GROUP + q * 8 + xr) * RT_WORDS;
+        const int32_t* rtb = rta + 32 * RT_WORDS;
+        const uint32_t code = (uint32_t)rta[0];
+        const uint32_t gs0 = (uint32_t)rta[1], gs1 = (uint32_t)rta[2];
         auto foff = [&](int r) {
             r = min(r, nsh - 1);
             return (uint32_t)(r * 128 + ((ax ^ (r & 7)) << 4)) ^ kx;
         };
         const uint32_t oi0 = foff((int)(code & 0xffu)), oi1 = foff((int)((code >> 8) & 0xffu));
         const bool reload = gs1 != gs0;
-        uint32_t oj0[4];
+        uint32_t oj0[4], ojb[4];
 #pragma unroll
         for (int y = 0; y < 4; ++y) oj0[y] = foff((int)((gs0 >> (8 * y)) & 0xffu));
-        // this thread's A_lo byte offset inside a tile block for k-step
-        // kstep (k-step kstep + 2 of the second half: k-groups 4 further,
-        // + 512 bytes): row 32q + xr (y = 0), k-group 2 kstep + ax / 2,
-        // bytes (ax % 2) * 8
-        const int alo_thr = (4 * q) * 1024 + (2 * kstep + (ax >> 1)) * 128 + xr * 16 + (ax & 1) * 8;
+        const uint32_t gsb = (uint32_t)rtb[1];
+        const uint32_t oib = foff((int)((uint32_t)rtb[0] & 0xffu));
+#pragma unroll
+        for (int y = 0; y < 4; ++y) ojb[y] = foff((int)((gsb >> (8 * y)) & 0xffu));
+        // this thread's A_lo byte offset inside a tile block for k-step ks:
+        // row 32q + xr (y = 0), k-group 2 ks + ax / 2, bytes (ax % 2) * 8
+        const int alo_thr = (4 * q) * 1024 + (2 * ks + (ax >> 1)) * 128 + xr * 16 + (ax & 1) * 8;
         // B writer: shell r, k-group g (voxels 8g..8g+7 of the 64); 8 nshell <= 512 threads
         int ub_r = -1, ub_g = 0;
-        const bool b_warp = (warp * 32) < nsh * 8;
         if (tid < nsh * 8) {
             ub_g = tid / nsh;
             ub_r = tid - ub_g * nsh;
@@ -980,33 +983,29 @@ contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ C
                 if constexpr (RES) split_store8_res(x, Bst + op_off64(brow(ub_r, 0), ub_g), Bst + op_off64(brow(ub_r, 1), ub_g));
                 else split_store8(x, Bst + op_off64(brow(ub_r, 0), ub_g), Bst + op_off64(brow(ub_r, 1), ub_g));
             }
-            if (tp_on) {
+            {
+                const unsigned char* Fh = F + hh * F_BYTES;
+                const float4 fi0 = lds4(Fh, oi0);
+                const float4 fi1 = lds4(Fh, oi1);
+                float4 fj[4];
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const unsigned char* Fh = F + h * F_BYTES;
-                    const int ks = kstep + 2 * h;
-                    const float4 fi0 = lds4(Fh, oi0);
-                    const float4 fi1 = slot1_on ? lds4(Fh, oi1) : fi0;
-                    float4 fj[4];
+                for (int y = 0; y < 4; ++y) fj[y] = lds4(Fh, oj0[y]);
+                store_slot64<RES>(fi0, fj, lane_base + acol(s, 0, ks), Alo + alo_thr);
+                if (reload) {
 #pragma unroll
-                    for (int y = 0; y < 4; ++y) fj[y] = lds4(Fh, oj0[y]);
-                    if (tp == 0)
-                        store_slot64<RES>(fi0, fj, lane_base + acol(s, 0, ks), Alo + alo_thr + h * 512);
-                    else
-                        store_slot64_tmem<RES>(fi0, fj, lane_base + acol(s, 2, ks), lane_base + acol(s, 3, ks));
-                    if (slot1_on) {
-                        if (reload) {
+                    for (int y = 0; y < 4; ++y) fj[y] = lds4(Fh, foff((int)((gs1 >> (8 * y)) & 0xffu)));
+                }
+                store_slot64<RES>(fi1, fj, lane_base + acol(s, 1, ks), Alo + ALO_TILE_BYTES + alo_thr);
+                if (b_on) {
+                    const float4 fb = lds4(Fh, oib);
 #pragma unroll
-                            for (int y = 0; y < 4; ++y) fj[y] = lds4(Fh, foff((int)((gs1 >> (8 * y)) & 0xffu)));
-                        }
-                        store_slot64<RES>(fi1, fj, lane_base + acol(s, 2 * tp + 1, ks),
-                                     Alo + (2 * tp + 1) * ALO_TILE_BYTES + alo_thr + h * 512);
-                    }
+                    for (int y = 0; y < 4; ++y) fj[y] = lds4(Fh, ojb[y]);
+                    store_slot64_tmem<RES>(fb, fj, lane_base + acol(s, 2, ks), lane_base + acol(s, 3, ks));
                 }
             }
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
             // A_lo and B writes (generic proxy) made visible to the MMA (async proxy)
-            if ((tp_on && (tp == 0 || ntl == 2)) || b_warp) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
             if (lane == 0) {
