@@ -208,6 +208,47 @@ __device__ __forceinline__ void dft_composite(C* v, int sign) {
     }
 }
 
+// Composite radices R = A*B with gcd(A, B) = 1 by the prime-factor
+// (Good-Thomas) mapping, which needs no inner twiddles: with input index
+// n = (B n1 + A n2) mod R and output index k the solution of k = k1 (mod A),
+// k = k2 (mod B),
+//   X[k] = DFT_B over n2 of ( DFT_A over n1 of x[(B n1 + A n2) mod R] )[k1]
+// (W_R^(nk) = W_A^(n1 k1) W_B^(n2 k2) for these index maps, since the cross
+// terms are multiples of R).  All index maps are compile-time constants.
+constexpr int crt_index(int k1, int A, int k2, int B) {
+    int k = 0;
+    while (k % A != k1 || k % B != k2) ++k;
+    return k;
+}
+
+template <typename T, typename C, int A, int B>
+__device__ __forceinline__ void dft_pfa(C* v, int sign) {
+    constexpr int R = A * B;
+    C y[R];
+    static_for<B>([&](auto n2c) {
+        constexpr int n2 = decltype(n2c)::value;
+        C t[A];
+        static_for<A>([&](auto n1c) {
+            constexpr int n1 = decltype(n1c)::value;
+            t[n1] = v[(B * n1 + A * n2) % R];
+        });
+        small_dft<T, C, A>(t, sign);
+#pragma unroll
+        for (int k1 = 0; k1 < A; ++k1) y[n2 * A + k1] = t[k1];
+    });
+    static_for<A>([&](auto k1c) {
+        constexpr int k1 = decltype(k1c)::value;
+        C u[B];
+#pragma unroll
+        for (int n2 = 0; n2 < B; ++n2) u[n2] = y[n2 * A + k1];
+        small_dft<T, C, B>(u, sign);
+        static_for<B>([&](auto k2c) {
+            constexpr int k2 = decltype(k2c)::value;
+            v[crt_index(k1, A, k2, B)] = u[k2];
+        });
+    });
+}
+
 template <typename T, typename C, int R>
 __device__ __forceinline__ void small_dft(C* v, int sign) {
     if constexpr (R == 2) dft2<T>(v);
@@ -215,15 +256,15 @@ __device__ __forceinline__ void small_dft(C* v, int sign) {
     else if constexpr (R == 4) dft4<T>(v, sign);
     else if constexpr (R == 5) dft5<T>(v, sign);
     else if constexpr (R == 8) dft8<T>(v, sign);
-    else if constexpr (R == 6) dft_composite<T, C, 3, 2>(v, sign);
+    else if constexpr (R == 6) dft_pfa<T, C, 3, 2>(v, sign);
     else if constexpr (R == 9) dft_composite<T, C, 3, 3>(v, sign);
-    else if constexpr (R == 10) dft_composite<T, C, 5, 2>(v, sign);
-    else if constexpr (R == 12) dft_composite<T, C, 4, 3>(v, sign);
-    else if constexpr (R == 15) dft_composite<T, C, 5, 3>(v, sign);
+    else if constexpr (R == 10) dft_pfa<T, C, 5, 2>(v, sign);
+    else if constexpr (R == 12) dft_pfa<T, C, 4, 3>(v, sign);
+    else if constexpr (R == 15) dft_pfa<T, C, 5, 3>(v, sign);
     else if constexpr (R == 16) dft_composite<T, C, 4, 4>(v, sign);
-    else if constexpr (R == 20) dft_composite<T, C, 5, 4>(v, sign);
-    else if constexpr (R == 18) dft_composite<T, C, 6, 3>(v, sign);
-    else if constexpr (R == 24) dft_composite<T, C, 8, 3>(v, sign);
+    else if constexpr (R == 20) dft_pfa<T, C, 5, 4>(v, sign);
+    else if constexpr (R == 18) dft_pfa<T, C, 9, 2>(v, sign);
+    else if constexpr (R == 24) dft_pfa<T, C, 8, 3>(v, sign);
     else static_assert(R == 2, "unsupported radix");
 }
 
