@@ -151,8 +151,11 @@ def test_config1_uniform_128_end_to_end():
         # the shot-noise field of the uniform box is less forgiving than the
         # clustered 360^3 box (where split-BF16 stays below 1e-5 / 2e-7): here
         # the worst triangles of condition number ~1e3 reach 1.3e-5 with
-        # either drain interval (measured 1.30e-5 / 1.24e-5), so the bound is 2e-5
-        bound = {"fp32": (2e-6, 3e-8), "bf16x3": (2e-5, 3e-7), "bf16x3_fine": (2e-5, 1e-7),
+        # either drain interval (measured 1.30e-5 / 1.24e-5), so the bound is 2e-5.
+        # FP32: the mesh accumulates particles with float atomics, so delta(k)
+        # -- and with it the worst triangle -- changes in its last bits from
+        # run to run (measured 1.78e-6 and 2.36e-6 on two runs of one build)
+        bound = {"fp32": (4e-6, 3e-8), "bf16x3": (2e-5, 3e-7), "bf16x3_fine": (2e-5, 1e-7),
                  "bf16x6": (1e-5, 1e-7)}[method]
         assert con["max_rel_cond_lt_1e3"] <= bound[0]
         assert con["normalised_max"] <= bound[1]
