@@ -88,7 +88,8 @@ def plan_info(nmax, ncut, step):
 def fp32_tiles(nmax, ncut, step):
     """Micro-tiles (4 pair rows x 8 shells) of the FP32 contraction's plan for
     the triangle loop: pairs (i, j) sorted by (j, i) in groups of 4, one tile
-    per 8-wide window of l between the group's lowest and highest l."""
+    per aligned 8-wide window of l (l0 a multiple of 8) that meets the group's
+    l range."""
     jmin = ncut // step
     pairs = {}
     for i in range(jmin, nmax + 1):
@@ -100,7 +101,7 @@ def fp32_tiles(nmax, ncut, step):
     for g in range(0, len(order), 4):
         ls = [l for p in order[g:g + 4] for l in pairs[p]]
         lo, hi = min(ls), max(ls)
-        tiles += (hi - lo) // 8 + 1
+        tiles += hi // 8 - lo // 8 + 1
     return tiles
 
 

@@ -136,15 +136,33 @@ template int contract_simple_impl<double>(const double*, int64_t, int, const int
 // ---------------------------------------------------------------------------
 // FP32 CUDA-core contraction, register-tiled.  Triangles are grouped as
 // (pair (i, j), shell l) like the tensor-core form: pairs sorted by (j, i),
-// four consecutive pairs x eight consecutive l form one thread's micro-tile
-// (32 accumulators).  Per voxel pair a thread loads 16 float2 values, forms 4
-// pair products and issues 32 packed FP32x2 FMAs.  Voxel chunks are staged in
-// shared memory with cp.async (double-buffered); each chunk's FP32 sums are
-// folded into Kahan-compensated FP32 totals; CTAs write float64 partials.
+// four consecutive pairs x one aligned window of eight shells l (l0 a
+// multiple of 8) form one thread's micro-tile (32 accumulators).  The
+// threads of a warp hold consecutive micro-tiles, so the lanes of one pair
+// group read the same F_i, F_j words (shared-memory broadcast) and a warp's
+// window rows are at most five distinct rows per load.
+//
+// Voxel chunks of every shell are staged in shared memory by bulk copies
+// that one producer warp issues (double-buffered; "full" mbarriers complete
+// with the copies, "empty" ones when every compute warp is done with a
+// buffer, so no warp waits for another's compute); row r starts at r * RS + 4 * ((r +
+// r / 8) % 8) floats, so rows that differ in r % 8 or in r / 8 start in
+// different 16-byte bank groups.  Per four voxels a thread loads its eight
+// window rows and four (F_i, F_j) pairs and issues 64 packed FP32x2 FMAs;
+// each chunk's sums are folded into Kahan-compensated FP32 totals held in
+// shared memory; CTAs write float64 partials.
 // ---------------------------------------------------------------------------
 namespace simt {
-constexpr int MT = 4, NT = 8, VC = 128, FS = VC + 2;   // padded row of the staging buffer
-constexpr int MAXT = 384;                               // micro-tiles per CTA (threads; 168 registers each)
+constexpr int MT = 4, NT = 8, VC = 128;
+constexpr int RS = VC + 32;                             // floats per staged row incl. its bank shift
+constexpr int MAXT = 352;                               // micro-tiles (compute threads) per CTA
+constexpr int THREADS_MAX = MAXT + 32;                  // + the producer warp
+__host__ __device__ constexpr int row_off(int r) { return r * RS + 4 * ((r + (r >> 3)) & 7); }
+// floats of one staging buffer: nshell field rows and NT zero rows
+__host__ __device__ constexpr size_t buf_floats(int nshell) { return (size_t)(nshell + NT) * RS; }
+__host__ __device__ constexpr size_t fp32_smem(int nshell, int threads) {
+    return 2 * buf_floats(nshell) * sizeof(float) + (size_t)MT * NT * threads * sizeof(float2);
+}
 
 struct Params {
     const float* fields;
@@ -173,89 +191,166 @@ __device__ __forceinline__ float2 mul2(float2 a, float2 b) {
         : "l"(*reinterpret_cast<unsigned long long*>(&a)), "l"(*reinterpret_cast<unsigned long long*>(&b)));
     return r;
 }
+__device__ __forceinline__ float4 lds4f(const float* p) { return *reinterpret_cast<const float4*>(p); }
 
-__global__ void __launch_bounds__(MAXT, 1) contract_fp32_kernel(const __grid_constant__ Params P) {
-    extern __shared__ __align__(16) float sbuf[];       // 2 x (nshell + NT) x FS
-    const int tid = threadIdx.x;
-    const int rowsz = (P.nshell + NT) * FS;
+// bounded wait on an mbarrier phase (~2 s of globaltimer), false on timeout
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
+    unsigned long long t0 = 0;
+    for (uint32_t it = 0;; ++it) {
+        uint32_t ok;
+        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+        if (ok) return true;
+        if ((it & 255u) == 0) {
+            unsigned long long t;
+            asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+            if (t0 == 0) t0 = t;
+            else if (t - t0 > 2000000000ull) return false;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(THREADS_MAX, 1) contract_fp32_kernel(const __grid_constant__ Params P) {
+    extern __shared__ __align__(16) float sbuf[];        // 2 staging buffers, then the Kahan state
+    __shared__ __align__(8) uint64_t full[2], empty[2];
+    __shared__ int abort_flag_s;
+    volatile int& abort_flag = abort_flag_s;
+    const int tid = threadIdx.x, nthr = P.tiles_per_cta;  // compute threads; the producer warp follows
+    const int ncw = nthr / 32;
+    const size_t BUF = buf_floats(P.nshell);
+    float2* kahan = reinterpret_cast<float2*>(sbuf + 2 * BUF);   // [32][nthr]: (sum, compensation)
     const int tile = blockIdx.y * P.tiles_per_cta + tid;
-    const bool valid = tid < P.tiles_per_cta && tile < P.ntile;
-    const int zero_row = P.nshell * FS;                  // never written by the copies
-    // rows nshell .. nshell+NT-1 of both buffers are zero and never copied into
-    for (int i = tid; i < NT * FS; i += blockDim.x) { sbuf[zero_row + i] = 0.f; sbuf[rowsz + zero_row + i] = 0.f; }
-    int fi[MT], fj[MT];
+    const bool valid = tid < nthr && tile < P.ntile;
+    // rows nshell .. nshell + NT - 1 of both buffers stay zero (never copied into)
+    for (size_t i = tid; i < 2 * BUF; i += blockDim.x) sbuf[i] = 0.f;
+    for (int i = tid; i < MT * NT * nthr; i += blockDim.x) kahan[i] = make_float2(0.f, 0.f);
+    const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(&full[0]);
+    const uint32_t ebar0 = (uint32_t)__cvta_generic_to_shared(&empty[0]);
+    if (tid == 0) {
+        abort_flag = 0;
+        for (int b = 0; b < 2; ++b) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar0 + 8u * b), "r"(1));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(ebar0 + 8u * b), "r"(ncw));
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // the zero fill (generic proxy) is ordered before the bulk copies (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    int oi[MT], oj[MT], ol[NT];
 #pragma unroll
     for (int k = 0; k < MT; ++k) {
         const int i = valid ? P.tile_rows[(size_t)tile * 8 + k] : -1;
         const int j = valid ? P.tile_rows[(size_t)tile * 8 + 4 + k] : -1;
-        fi[k] = i >= 0 ? i * FS : zero_row;
-        fj[k] = j >= 0 ? j * FS : zero_row;
+        oi[k] = row_off(i >= 0 ? i : P.nshell);
+        oj[k] = row_off(j >= 0 ? j : P.nshell);
     }
-    // l0 + m <= nshell + NT - 1 always stays inside the buffer
-    const int fl0 = (valid ? P.tile_l0[tile] : P.nshell) * FS;
-    float hi[MT * NT], lo[MT * NT];
+    {
+        // l0 is a multiple of NT and l0 + NT - 1 < nshell + NT: inside the buffer
+        const int l0 = valid ? P.tile_l0[tile] : P.nshell / NT * NT;
 #pragma unroll
-    for (int e = 0; e < MT * NT; ++e) { hi[e] = 0.f; lo[e] = 0.f; }
-
+        for (int m = 0; m < NT; ++m) ol[m] = row_off(l0 + m);
+    }
     const int64_t c0 = (int64_t)blockIdx.x * P.chunks_per_cta;
     const int64_t c1 = min(P.nchunks, c0 + P.chunks_per_cta);
     const int nch = (int)max((int64_t)0, c1 - c0);
-    const int ncp = P.nshell * (VC / 4);
-    auto issue = [&](int c, int buf) {
-        const int64_t vbase = (c0 + c) * VC;
-        for (int u = tid; u < ncp; u += blockDim.x) {
-            const int s = u / (VC / 4), q = u - s * (VC / 4);
-            const int64_t v = vbase + 4 * q;
-            int bytes = 0;
-            if (v < P.V) bytes = (int)min((int64_t)16, (P.V - v) * 4);
-            const float* src = P.fields + (size_t)s * P.V + (bytes > 0 ? v : 0);
-            const uint32_t dst = (uint32_t)__cvta_generic_to_shared(sbuf + buf * rowsz + s * FS + 4 * q);
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" :: "r"(dst), "l"(src),
-                         "r"(bytes > 8 ? 8 : bytes) : "memory");
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" :: "r"(dst + 8), "l"(src + 2),
-                         "r"(bytes > 8 ? bytes - 8 : 0) : "memory");
-        }
-        asm volatile("cp.async.commit_group;" ::: "memory");
+    // the producer: chunk c of this CTA into buffer b, one bulk copy per shell row
+    auto issue = [&](int c, int b) {
+        const int64_t v0 = (c0 + c) * VC;
+        const uint32_t bytes = (uint32_t)(min((int64_t)VC, P.V - v0) * 4);
+        const uint32_t bar = bar0 + 8u * b;
+        const uint32_t dst0 = (uint32_t)__cvta_generic_to_shared(sbuf + (size_t)b * BUF);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(bytes * P.nshell)
+                     : "memory");
+        for (int r = 0; r < P.nshell; ++r)
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         :: "r"(dst0 + 4u * (uint32_t)row_off(r)), "l"(P.fields + (size_t)r * P.V + v0), "r"(bytes),
+                            "r"(bar)
+                         : "memory");
     };
-    if (nch > 0) issue(0, 0);
+    if (tid >= nthr) {
+        // ================= producer warp =================
+        if (tid == nthr) {
+            int c = 0;
+            for (; c < nch; ++c) {
+                const int b = c & 1;
+                if (c >= 2) {
+                    if (!bar_wait(ebar0 + 8u * b, (uint32_t)((c - 2) >> 1) & 1u) || abort_flag) {
+                        abort_flag = 1;
+                        break;
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                }
+                issue(c, b);
+            }
+            // no copy may land after the CTA exits: wait (bounded) for the last ones
+            for (int k = max(0, c - 2); k < c; ++k) (void)bar_wait(bar0 + 8u * (k & 1), (uint32_t)(k >> 1) & 1u);
+        }
+        return;
+    }
+    // ================= compute warps =================
+    bool ok = true;
     for (int c = 0; c < nch; ++c) {
-        asm volatile("cp.async.wait_group 0;" ::: "memory");
-        __syncthreads();
-        if (c + 1 < nch) issue(c + 1, (c + 1) & 1);
-        const float* F = sbuf + (c & 1) * rowsz;
-        float2 cur[MT * NT];
-#pragma unroll
-        for (int e = 0; e < MT * NT; ++e) cur[e] = make_float2(0.f, 0.f);
+        const int b = c & 1;
+        if (!__all_sync(0xffffffffu, bar_wait(bar0 + 8u * b, (uint32_t)(c >> 1) & 1u)) || abort_flag) {
+            abort_flag = 1;
+            ok = false;
+            break;
+        }
+        const float* F = sbuf + (size_t)b * BUF;
+        const int nq = (int)(min((int64_t)VC, P.V - (c0 + c) * VC) / 4);
         if (valid) {
-#pragma unroll 2
-            for (int v = 0; v < VC; v += 2) {
-                float2 pp[MT], ll[NT];
+            float2 acc[MT * NT];
 #pragma unroll
-                for (int k = 0; k < MT; ++k)
-                    pp[k] = mul2(*reinterpret_cast<const float2*>(F + fi[k] + v),
-                                 *reinterpret_cast<const float2*>(F + fj[k] + v));
+            for (int e = 0; e < MT * NT; ++e) acc[e] = make_float2(0.f, 0.f);
+#pragma unroll 1
+            for (int q = 0; q < nq; ++q) {
+                const int o = 4 * q;
+                float4 fl[NT];
 #pragma unroll
-                for (int m = 0; m < NT; ++m) ll[m] = *reinterpret_cast<const float2*>(F + fl0 + m * FS + v);
+                for (int m = 0; m < NT; ++m) fl[m] = lds4f(F + ol[m] + o);
 #pragma unroll
-                for (int k = 0; k < MT; ++k)
+                for (int k = 0; k < MT; ++k) {
+                    const float4 a = lds4f(F + oi[k] + o), bb = lds4f(F + oj[k] + o);
+                    const float2 p0 = mul2(make_float2(a.x, a.y), make_float2(bb.x, bb.y));
+                    const float2 p1 = mul2(make_float2(a.z, a.w), make_float2(bb.z, bb.w));
 #pragma unroll
-                    for (int m = 0; m < NT; ++m) cur[k * NT + m] = fma2(pp[k], ll[m], cur[k * NT + m]);
+                    for (int m = 0; m < NT; ++m) {
+                        acc[k * NT + m] = fma2(p0, make_float2(fl[m].x, fl[m].y), acc[k * NT + m]);
+                        acc[k * NT + m] = fma2(p1, make_float2(fl[m].z, fl[m].w), acc[k * NT + m]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int e = 0; e < MT * NT; ++e) {   // Kahan fold of the chunk sum
+                float2 h = kahan[e * nthr + tid];
+                const float y = (acc[e].x + acc[e].y) - h.y;
+                const float t = h.x + y;
+                h.y = (t - h.x) - y;
+                h.x = t;
+                kahan[e * nthr + tid] = h;
             }
         }
-#pragma unroll
-        for (int e = 0; e < MT * NT; ++e) {   // Kahan fold of the chunk sum
-            const float y = (cur[e].x + cur[e].y) - lo[e];
-            const float t = hi[e] + y;
-            lo[e] = (t - hi[e]) - y;
-            hi[e] = t;
+        __syncwarp();      // this warp is done with buffer b
+        if ((tid & 31) == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(ebar0 + 8u * b) : "memory");
+    }
+    if (!ok) {
+        // a copy never completed: report NaN partials for this warp's triangles
+        if (valid) {
+#pragma unroll 1
+            for (int e = 0; e < MT * NT; ++e) {
+                const int t = P.tile_tri[(size_t)tile * 32 + e];
+                if (t >= 0) P.partials[(size_t)blockIdx.x * P.ntri + t] = __longlong_as_double(0x7ff8000000000000ll);
+            }
         }
-        __syncthreads();   // everyone is done with buffer c&1 before it is refilled
+        return;
     }
     if (valid) {
 #pragma unroll
         for (int e = 0; e < MT * NT; ++e) {
             const int t = P.tile_tri[(size_t)tile * 32 + e];
-            if (t >= 0) P.partials[(size_t)blockIdx.x * P.ntri + t] = (double)hi[e] - (double)lo[e];
+            const float2 h = kahan[e * nthr + tid];
+            if (t >= 0) P.partials[(size_t)blockIdx.x * P.ntri + t] = (double)h.x - (double)h.y;
         }
     }
 }
@@ -308,7 +403,7 @@ static HostPlan* plan(int nshell, const int32_t* tri_host, int ntri) {
         int lo = 1 << 30, hi = -1;
         for (size_t r = g; r < std::min(order.size(), g + MT); ++r)
             for (auto& lt : pairs[order[r]]) { lo = std::min(lo, lt.first); hi = std::max(hi, lt.first); }
-        for (int l0 = lo; l0 <= hi; l0 += NT) {
+        for (int l0 = lo / NT * NT; l0 <= hi; l0 += NT) {
             int16_t rr[8];
             int32_t tt[32];
             for (int e = 0; e < 32; ++e) tt[e] = -1;
@@ -339,13 +434,23 @@ static HostPlan* plan(int nshell, const int32_t* tri_host, int ntri) {
     return hp;
 }
 
-static void grid_dims(int64_t nvox, int ntile, int* gx, int* gy, int* per) {
-    *gy = std::max(1, (ntile + MAXT - 1) / MAXT);
+// threads (micro-tiles) per CTA that the shared memory leaves room for
+static int max_tiles(int nshell) {
+    const size_t lim = 227 * 1024, bufs = 2 * buf_floats(nshell) * sizeof(float);
+    if (bufs >= lim) return 0;
+    return std::min<int>(MAXT, (int)((lim - bufs) / (MT * NT * sizeof(float2))) / 32 * 32);
+}
+
+static bool grid_dims(int64_t nvox, int nshell, int ntile, int* gx, int* gy, int* per) {
+    const int mt = max_tiles(nshell);
+    if (mt < 32) return false;
+    *gy = std::max(1, (ntile + mt - 1) / mt);
     *per = ((ntile + *gy - 1) / *gy + 31) / 32 * 32;
     int sms = 152, dev = 0;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int64_t nch = (nvox + VC - 1) / VC;
     *gx = (int)std::max<int64_t>(1, std::min<int64_t>(nch, std::max(1, sms / *gy)));
+    return true;
 }
 
 // The cached plan of a list, or nullptr (never plans, never allocates).
@@ -377,7 +482,10 @@ int contract_fp32_need(int64_t nvox, int nshell, const int32_t* tri_host, int nt
         return PYSPEC_E_INVALID;
     }
     int gx, gy, per;
-    grid_dims(nvox, hp->ntile, &gx, &gy, &per);
+    if (!grid_dims(nvox, nshell, hp->ntile, &gx, &gy, &per)) {
+        set_error("%d shells do not fit the FP32 contraction's shared-memory staging", nshell);
+        return PYSPEC_E_UNSUPPORTED;
+    }
     *need = hp->image.size() + al((size_t)gx * ntri * sizeof(double));
     return PYSPEC_OK;
 }
@@ -408,7 +516,10 @@ int contract_fp32_impl(const float* fields, int64_t nvox, int nshell, const int3
         return PYSPEC_E_INVALID;
     }
     int gx, gy, per;
-    grid_dims(nvox, hp->ntile, &gx, &gy, &per);
+    if (!grid_dims(nvox, nshell, hp->ntile, &gx, &gy, &per)) {
+        set_error("%d shells do not fit the FP32 contraction's shared-memory staging", nshell);
+        return PYSPEC_E_UNSUPPORTED;
+    }
     char* w = reinterpret_cast<char*>(ws);
     size_t off = 0;
     int16_t* d_rows = reinterpret_cast<int16_t*>(w + off);
@@ -436,9 +547,9 @@ int contract_fp32_impl(const float* fields, int64_t nvox, int nshell, const int3
     P.nchunks = (nvox + VC - 1) / VC;
     P.chunks_per_cta = (P.nchunks + gx - 1) / gx;
     P.partials = partials;
-    const size_t sm = sizeof(float) * 2 * (size_t)(nshell + NT) * FS;
+    const size_t sm = fp32_smem(nshell, per);
     PYSPEC_TRY(allow_smem((const void*)contract_fp32_kernel, sm));
-    contract_fp32_kernel<<<dim3(gx, gy), per, sm, st>>>(P);
+    contract_fp32_kernel<<<dim3(gx, gy), per + 32, sm, st>>>(P);   // + the producer warp
     PYSPEC_LAUNCH_CHECK();
     count_launch();
     return reduce_partials_launch(partials, gx, ntri, bsum, st);
