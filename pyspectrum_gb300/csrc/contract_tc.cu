@@ -690,6 +690,9 @@ constexpr int STAGE64_BYTES = BROWS * KC64 * 2;     // B operand of one stage: 1
 constexpr int ALO_TILE_BYTES = 128 * KC64 * 2;      // A_lo of one tile and stage: 16 KB
 constexpr int SEG64_SHIFT = 1;                       // drains every 2^(seg_log2 - 1) deep chunks (same voxels)
 constexpr int kDeepSmemLimit = 232448 - 6144;        // dynamic bytes: the 227 KB opt-in less the static arrays
+constexpr int NBW64 = 2;                             // B-operand writer warps, after the MMA and copy warps
+constexpr int BW0 = PWARPS + 2;
+constexpr int NTHREADS64 = NTHREADS + 32 * NBW64;
 
 // A_lo blocks in shared memory: tiles 0 and 1 (tile 2 keeps its A_lo in
 // TMEM, in the columns of the absent tile 3)
@@ -808,10 +811,13 @@ __device__ __forceinline__ void issue_chunk64(const uint32_t (&dcol)[MAXTILES], 
     }
 }
 
-template <int NFB, bool RES = false>
-__global__ void __launch_bounds__(NTHREADS, 1)
+template <int NFB, bool RES = false, bool BW = false>
+__global__ void __launch_bounds__(BW ? NTHREADS64 : NTHREADS, 1)
 contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ CUtensorMap fmap) {
-    // RES: the residual pass of the 6-product form (narrow accumulators)
+    // RES: the residual pass of the 6-product form (narrow accumulators);
+    // BW: NBW64 extra warps write the B operand (else the producers do)
+    constexpr int NTH = BW ? NTHREADS64 : NTHREADS;
+    constexpr int NARR = PWARPS + (BW ? NBW64 : 0);      // arrivals per chunk on bar_full / bar_fempty
     extern __shared__ unsigned char smem_raw[];
     __shared__ Group G;
     __shared__ __align__(8) uint64_t bar_full[NSTAGE], bar_empty[NSTAGE], bar_ffull[NFB], bar_fempty[NFB];
@@ -840,19 +846,19 @@ contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ C
     int C = 0;
     for (int t = 0; t < ntl; ++t) C = max(C, G.tile_col[t] + (RES ? 1 : 2) * G.tile_n[t]);
 
-    for (int i = tid; i < MAXROWS * 4; i += NTHREADS) pij[i] = P.pair_row[(size_t)G.table_off * 4 + i];
-    for (int i = tid; i < G.nslots; i += NTHREADS) acc[i] = make_float2(0.f, 0.f);
-    for (int i = tid; i < NSTAGE * STAGE64_BYTES / 16; i += NTHREADS)
+    for (int i = tid; i < MAXROWS * 4; i += NTH) pij[i] = P.pair_row[(size_t)G.table_off * 4 + i];
+    for (int i = tid; i < G.nslots; i += NTH) acc[i] = make_float2(0.f, 0.f);
+    for (int i = tid; i < NSTAGE * STAGE64_BYTES / 16; i += NTH)
         reinterpret_cast<uint4*>(stage_base)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
         abort_flag = 0;
         for (int s = 0; s < NSTAGE; ++s) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_full[s])), "r"(PWARPS));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_full[s])), "r"(NARR));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_empty[s])), "r"(1));
         }
         for (int b = 0; b < NFB; ++b) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_ffull[b])), "r"(1));
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_fempty[b])), "r"(PWARPS));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_fempty[b])), "r"(NARR));
         }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_seg)), "r"(1));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_drained)), "r"(PWARPS));
@@ -908,9 +914,10 @@ contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ C
         // this thread's A_lo byte offset inside a tile block for k-step ks:
         // row 32q + xr (y = 0), k-group 2 ks + ax / 2, bytes (ax % 2) * 8
         const int alo_thr = (4 * q) * 1024 + (2 * ks + (ax >> 1)) * 128 + xr * 16 + (ax & 1) * 8;
-        // B writer: shell r, k-group g (voxels 8g..8g+7 of the 64); 8 nshell <= 512 threads
+        // without B-writer warps the producers write the B operand: shell r,
+        // k-group g (voxels 8g..8g+7 of the 64); 8 nshell <= 512 threads
         int ub_r = -1, ub_g = 0;
-        if (tid < nsh * 8) {
+        if (!BW && tid < nsh * 8) {
             ub_g = tid / nsh;
             ub_r = tid - ub_g * nsh;
         }
@@ -971,9 +978,9 @@ contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ C
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             }
             const unsigned char* F = fbuf + (size_t)b * 2 * F_BYTES;
-            char* Bst = reinterpret_cast<char*>(stage_base) + (size_t)s * STAGE64_BYTES;
             char* Alo = reinterpret_cast<char*>(alo_base) + (size_t)s * nlo * ALO_TILE_BYTES;
             if (ub_r >= 0) {
+                char* Bst = reinterpret_cast<char*>(stage_base) + (size_t)s * STAGE64_BYTES;
                 const unsigned char* Fh = F + (ub_g >> 2) * F_BYTES;
                 const int g4 = ub_g & 3;
                 const float4 a = *reinterpret_cast<const float4*>(Fh + fchunk(ub_r, 2 * g4));
@@ -1061,6 +1068,63 @@ contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ C
                 mbar_wait(smem_u32(&bar_seg), seg_count & 1);
             }
         }
+    } else if (BW && warp >= BW0) {
+        // ================= B writers =================
+        // item (shell r, k-group g: voxels 8g .. 8g + 7 of the 64): its hi and
+        // lo rows of the stage's B operand; items bt, bt + 64, ... (8 nshell <= 512)
+        const int bt = tid - BW0 * 32;
+        const int nsh = P.nshell;
+        constexpr int MAXIT = 8 * MAXB / (32 * NBW64);
+        uint32_t src0[MAXIT], src1[MAXIT], dhi[MAXIT], dlo[MAXIT];
+        int nit = 0;
+#pragma unroll
+        for (int k = 0; k < MAXIT; ++k) {
+            const int it = bt + 32 * NBW64 * k;
+            const int g = it / nsh, r = it - g * nsh;
+            if (it < 8 * nsh) nit = k + 1;
+            src0[k] = (uint32_t)((g >> 2) * F_BYTES + fchunk(r, 2 * (g & 3)));
+            src1[k] = (uint32_t)((g >> 2) * F_BYTES + fchunk(r, 2 * (g & 3) + 1));
+            dhi[k] = (uint32_t)op_off64(brow(r, 0), g);
+            dlo[k] = (uint32_t)op_off64(brow(r, 1), g);
+        }
+        for (int c = 0; c < nch; ++c) {
+            if (__any_sync(0xffffffffu, abort_flag != 0)) break;
+            const int s = c & 1;
+            const int b = c % NFB;
+            if (!warp_wait(smem_u32(&bar_ffull[b]), (uint32_t)(c / NFB) & 1u)) {
+                atomicExch(P.err, 1);
+                abort_flag = 1;
+                break;
+            }
+            if (c >= NSTAGE) {
+                if (!warp_wait(smem_u32(&bar_empty[s]), ((c - NSTAGE) >> 1) & 1)) {
+                    atomicExch(P.err, 1);
+                    abort_flag = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            }
+            const unsigned char* F = fbuf + (size_t)b * 2 * F_BYTES;
+            char* Bst = reinterpret_cast<char*>(stage_base) + (size_t)s * STAGE64_BYTES;
+#pragma unroll
+            for (int k = 0; k < MAXIT; ++k) {
+                if (k < nit) {
+                    const float4 a = *reinterpret_cast<const float4*>(F + src0[k]);
+                    const float4 e = *reinterpret_cast<const float4*>(F + src1[k]);
+                    const float2 x[4] = {make_float2(a.x, a.y), make_float2(a.z, a.w), make_float2(e.x, e.y),
+                                         make_float2(e.z, e.w)};
+                    if constexpr (RES) split_store8_res(x, Bst + dhi[k], Bst + dlo[k]);
+                    else split_store8(x, Bst + dhi[k], Bst + dlo[k]);
+                }
+            }
+            // B writes (generic proxy) made visible to the MMA (async proxy)
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(smem_u32(&bar_full[s]));
+                mbar_arrive(smem_u32(&bar_fempty[b]));
+            }
+        }
     } else if (warp == TMA_WARP && lane == 0) {
         // two 32-voxel copies per chunk into the buffer's halves, one barrier
         const uint32_t fb0 = smem_u32(fbuf);
@@ -1092,7 +1156,7 @@ contract_tc64_kernel(const __grid_constant__ Params P, const __grid_constant__ C
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (!abort_flag) {
-        for (int i = tid; i < G.nslots; i += NTHREADS) {
+        for (int i = tid; i < G.nslots; i += NTH) {
             const int t = P.slot_tri[(size_t)blockIdx.y * P.maxslots + i];
             if (t >= 0) P.partials[(size_t)blockIdx.x * P.ntri + t] = (double)acc[i].x - (double)acc[i].y;
         }
@@ -1130,6 +1194,7 @@ struct HostPlan {
     bool invalid = false;         // the triangle list itself is malformed (vs. unsupported)
     bool cover = false;           // rows are a pair cover (3 tiles), not runs
     int nfb64 = 0;                // field buffers of the 64-voxel kernel (0: the plan does not fit it)
+    bool bw64 = false;            // ... with B-writer warps (every group has 3 tiles, 3 field buffers)
     size_t smem64 = 0;            // its dynamic shared memory
     char why[160] = {0};
 };
@@ -1207,6 +1272,12 @@ static void finish_plan(HostPlan* hp, int ngroups, int maxslots, const std::vect
             hp->smem64 = need;
             break;
         }
+    }
+    // B-writer warps pay off when the producers form three tiles (measured at
+    // 360^3: 40 shells / 3 tiles 6.95 -> 6.79 ms; 30 shells / 2 tiles 5.16 -> 5.36)
+    if (hp->nfb64 == 3) {
+        hp->bw64 = true;
+        for (int g = 0; g < ngroups; ++g) hp->bw64 = hp->bw64 && P.g[g].ntiles == 3;
     }
 }
 
@@ -1729,6 +1800,25 @@ static EncodeTiledFn encode_tiled() {
     return fn;
 }
 
+// Launches the 64-voxel kernel for plan hp: with B-writer warps, or with
+// three or two field buffers.
+template <bool RES>
+static int launch_tc64(const tc::HostPlan* hp, const tc::Params& X, unsigned gx, cudaStream_t st,
+                       const CUtensorMap& fmap) {
+    using namespace tc;
+    const void* fn = hp->bw64 ? (const void*)contract_tc64_kernel<3, RES, true>
+                     : hp->nfb64 == 3 ? (const void*)contract_tc64_kernel<3, RES, false>
+                                      : (const void*)contract_tc64_kernel<2, RES, false>;
+    PYSPEC_TRY(allow_smem(fn, hp->smem64));
+    if (hp->bw64)
+        contract_tc64_kernel<3, RES, true><<<dim3(gx, X.ngroups), NTHREADS64, hp->smem64, st>>>(X, fmap);
+    else if (hp->nfb64 == 3)
+        contract_tc64_kernel<3, RES, false><<<dim3(gx, X.ngroups), NTHREADS, hp->smem64, st>>>(X, fmap);
+    else
+        contract_tc64_kernel<2, RES, false><<<dim3(gx, X.ngroups), NTHREADS, hp->smem64, st>>>(X, fmap);
+    return PYSPEC_OK;
+}
+
 int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_t* tri, const int32_t* tri_host,
                      int ntri, double* bsum, void* ws, size_t ws_bytes, cudaStream_t st, bool run_plan,
                      bool fine_drain, bool six, bool kc32) {
@@ -1801,12 +1891,7 @@ int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_
         Params D = P;
         D.nchunks = (nvox + KC64 - 1) / KC64;
         D.chunks_per_cta = (D.nchunks + gx - 1) / gx;
-        const void* fn = hp->nfb64 == 3 ? (const void*)contract_tc64_kernel<3> : (const void*)contract_tc64_kernel<2>;
-        PYSPEC_TRY(allow_smem(fn, hp->smem64));
-        if (hp->nfb64 == 3)
-            contract_tc64_kernel<3><<<dim3(gx, D.ngroups), NTHREADS, hp->smem64, st>>>(D, fmap);
-        else
-            contract_tc64_kernel<2><<<dim3(gx, D.ngroups), NTHREADS, hp->smem64, st>>>(D, fmap);
+        PYSPEC_TRY(launch_tc64<false>(hp, D, (unsigned)gx, st, fmap));
     } else {
         PYSPEC_TRY(allow_smem((const void*)contract_tc_kernel<false>, hp->smem));
         contract_tc_kernel<false><<<dim3(gx, P.ngroups), NTHREADS, hp->smem, st>>>(P, fmap);
@@ -1839,13 +1924,7 @@ int contract_tc_impl(const float* fields, int64_t nvox, int nshell, const int32_
             // 64-voxel chunks for this pass too
             R.nchunks = (nvox + KC64 - 1) / KC64;
             R.chunks_per_cta = (R.nchunks + gx - 1) / gx;
-            const void* fn = hp->nfb64 == 3 ? (const void*)contract_tc64_kernel<3, true>
-                                            : (const void*)contract_tc64_kernel<2, true>;
-            PYSPEC_TRY(allow_smem(fn, hp->smem64));
-            if (hp->nfb64 == 3)
-                contract_tc64_kernel<3, true><<<dim3(gx, R.ngroups), NTHREADS, hp->smem64, st>>>(R, fmap);
-            else
-                contract_tc64_kernel<2, true><<<dim3(gx, R.ngroups), NTHREADS, hp->smem64, st>>>(R, fmap);
+            PYSPEC_TRY(launch_tc64<true>(hp, R, (unsigned)gx, st, fmap));
         } else {
             PYSPEC_TRY(allow_smem((const void*)contract_tc_kernel<true>, hp->smem));
             contract_tc_kernel<true><<<dim3(gx, R.ngroups), NTHREADS, hp->smem, st>>>(R, fmap);
