@@ -204,6 +204,9 @@ int pyspec_shell_fields(const float *half, int ngrid, int step, int jmin, int nm
  *   fields 16-byte aligned, N^3 divisible by 4; returns PYSPEC_E_UNSUPPORTED
  *   otherwise).  After the stream has run a BF16X3 call, the int32 at
  *   workspace offset 0 is 0, or the code of a bounded wait that timed out.
+ *   The planned FP32 kernel stages its voxels with bulk copies under the
+ *   same bounded waits; if one times out, the triangles of the CTAs that
+ *   met it get bsum = NaN.
  * The triangles of one list must be distinct (as unordered shell triples):
  *   a repeated triangle returns PYSPEC_E_INVALID with either planned method.
  * ---------------------------------------------------------------------- */
