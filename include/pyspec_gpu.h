@@ -228,7 +228,8 @@ int pyspec_bk_contract(const float *fields, int ngrid, int nshell, const int32_t
  * slots of group 0, [5] 1 if group 0 uses the wide MMA form, [6] tensor-core
  * multiply-adds per voxel summed over groups (the executed work), [7] shared-
  * memory bank clashes between the producer threads that share load phases,
- * [8] voxels per chunk (64 or 32) the contraction runs with.
+ * [8] voxels per chunk (64 or 32) the contraction runs with, [9] 1 if that
+ * 64-voxel kernel has B-operand writer warps (plans of three tiles).
  * Returns 0; PYSPEC_E_INVALID / PYSPEC_E_UNSUPPORTED where the contraction
  * would; PYSPEC_E_INVALID with a message if the plan fails the check.
  * ---------------------------------------------------------------------- */

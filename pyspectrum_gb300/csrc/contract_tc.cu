@@ -2028,8 +2028,9 @@ extern "C" int pyspec_bk_plan_check_flags(int nshell, const int32_t* tri_host, i
             if (a[2] != a[1] || b[2] != b[1])
                 for (int y = 0; y < 4; ++y) clashes += clash((a[2] >> (8 * y)) & 0xff, (b[2] >> (8 * y)) & 0xff);
         }
-    const int64_t vals[9] = {P.ngroups, P.g[0].ntiles, hp->cover ? 1 : 0, mma, P.g[0].nslots, P.g[0].wide, macs,
-                             clashes, (hp->nfb64 > 0 && !(flags & PYSPEC_CONTRACT_KC32)) ? KC64 : KC};
-    for (int k = 0; k < ninfo && k < 9; ++k) info[k] = vals[k];
+    const bool deep = hp->nfb64 > 0 && !(flags & PYSPEC_CONTRACT_KC32);
+    const int64_t vals[10] = {P.ngroups, P.g[0].ntiles, hp->cover ? 1 : 0, mma, P.g[0].nslots, P.g[0].wide, macs,
+                              clashes, deep ? KC64 : KC, (deep && hp->bw64) ? 1 : 0};
+    for (int k = 0; k < ninfo && k < 10; ++k) info[k] = vals[k];
     return PYSPEC_OK;
 }

@@ -14,9 +14,10 @@ from pyspectrum_gb300 import _lib, core
 
 def plan_check(nshell, tri):
     tri = np.ascontiguousarray(tri, dtype=np.int32)
-    info = np.zeros(8, dtype=np.int64)
-    _lib.call("pyspec_bk_plan_check", int(nshell), tri.ctypes.data, int(tri.shape[1]), info.ctypes.data, 8)
-    return dict(zip(["groups", "tiles", "cover", "mma", "slots", "wide", "macs", "clashes"], info.tolist()))
+    info = np.zeros(10, dtype=np.int64)
+    _lib.call("pyspec_bk_plan_check", int(nshell), tri.ctypes.data, int(tri.shape[1]), info.ctypes.data, 10)
+    return dict(zip(["groups", "tiles", "cover", "mma", "slots", "wide", "macs", "clashes", "chunk", "bwarps"],
+                    info.tolist()))
 
 
 @pytest.mark.parametrize("nmax", [1, 2, 10, 20, 30, 36, 40, 45, 60, 64])
@@ -32,13 +33,15 @@ def test_bench_workload_gets_three_tiles():
     Nmax 30 fits 2."""
     info = plan_check(40, core.triangles(1, 40) - 1)
     assert info == {"groups": 1, "tiles": 3, "cover": 1, "mma": 12, "slots": info["slots"], "wide": 1,
-                    "macs": 3 * 128 * 2 * 2 * 40, "clashes": info["clashes"]}
+                    "macs": 3 * 128 * 2 * 2 * 40, "clashes": info["clashes"], "chunk": 64, "bwarps": 1}
     # producer threads that share load phases are paired to avoid bank clashes
     # (32 phase pairs x up to 8 loads; unpaired greedy order gave ~10x more)
     assert info["clashes"] <= 16
     # Nmax 30: 38 row threads of runs need 4 tiles; 32 two-slot cover blocks fit 2
     info30 = plan_check(30, core.triangles(1, 30) - 1)
     assert info30["cover"] == 1 and info30["tiles"] == 2 and info30["mma"] == 8
+    # 64-voxel chunks for both; B-operand writer warps only with three tiles
+    assert info30["chunk"] == 64 and info30["bwarps"] == 0
     # Nmax 20: runs already fit 2 tiles, no cover is searched
     info20 = plan_check(20, core.triangles(1, 20) - 1)
     assert info20["cover"] == 0 and info20["tiles"] == 2
