@@ -139,8 +139,11 @@ template int contract_simple_impl<double>(const double*, int64_t, int, const int
 // four consecutive pairs x one aligned window of eight shells l (l0 a
 // multiple of 8) form one thread's micro-tile (32 accumulators).  The
 // threads of a warp hold consecutive micro-tiles, so the lanes of one pair
-// group read the same F_i, F_j words (shared-memory broadcast) and a warp's
-// window rows are at most five distinct rows per load.
+// group read the same F_i, F_j words and a warp's window rows are at most
+// five distinct rows per load, which keeps bank conflicts rare.  (Sharing
+// does not cut the load cost itself: an LDS.128 takes four wavefronts
+// whatever its addresses, so the kernel's bound is the 2 bytes each lane
+// loads per FMA, half the FP32 FMA rate at 128 bytes per cycle per SM.)
 //
 // Voxel chunks of every shell are staged in shared memory by bulk copies
 // that one producer warp issues (double-buffered; "full" mbarriers complete
@@ -169,7 +172,7 @@ struct Params {
     int64_t V;
     int nshell;
     int ntile;                 // micro-tiles
-    int tiles_per_cta;         // threads per CTA (multiple of 32)
+    int tiles_per_cta;         // compute threads per CTA (multiple of 32); the producer warp follows
     const int16_t* tile_rows;  // [ntile][8]: i0..i3, j0..j3 (slot, -1 = empty row)
     const int16_t* tile_l0;    // [ntile]
     const int32_t* tile_tri;   // [ntile][32] triangle index or -1
@@ -292,7 +295,9 @@ __global__ void __launch_bounds__(THREADS_MAX, 1) contract_fp32_kernel(const __g
     bool ok = true;
     for (int c = 0; c < nch; ++c) {
         const int b = c & 1;
-        if (!__all_sync(0xffffffffu, bar_wait(bar0 + 8u * b, (uint32_t)(c >> 1) & 1u)) || abort_flag) {
+        // warp-uniform: every lane takes the same branch
+        const bool landed = __all_sync(0xffffffffu, bar_wait(bar0 + 8u * b, (uint32_t)(c >> 1) & 1u));
+        if (!landed || __any_sync(0xffffffffu, abort_flag != 0)) {
             abort_flag = 1;
             ok = false;
             break;
