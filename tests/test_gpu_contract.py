@@ -108,7 +108,8 @@ def test_chunk_tails(n, nmax):
     64-voxel chunk is partly past the end and the copies fill it with zeros;
     N = 50, Nmax 30 also has empty shells past the Nyquist shell) and grids
     with fewer chunks than CTAs (N = 18, 30): the 64- and 32-voxel
-    tensor-core forms against float64."""
+    tensor-core forms and the FP32 form (128-voxel chunks, the last one
+    partial at all three sizes) against float64."""
     jmin = 1
     fields = _fields(n, 1, jmin, nmax, seed=n)
     slots = np.ascontiguousarray(core.triangles(jmin, nmax) - jmin, dtype=np.int32)
@@ -123,6 +124,8 @@ def test_chunk_tails(n, nmax):
         assert status == 0
         err = np.abs(got - ref) / mag
         assert err.max() < 3e-5 and np.median(err) < 3e-6, flags
+    got32, _ = _contract(fields, n, slots, 0)
+    assert (np.abs(got32 - ref) / mag).max() < 1e-6
 
 
 def test_cover_plan_narrow_three_tiles():
